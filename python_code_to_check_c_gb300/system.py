@@ -1,0 +1,89 @@
+"""Seeded synthetic molecular systems (integral provider).
+
+The reference obtains its integrals from psi4 (``CCSD_Helper.py:26-93``:
+``mo_spin_eri``, ``F_MO``; dipoles at ``CCSD_Helper.py:970-980``).  psi4 is not
+available here, so systems are drawn from a seeded density-fitting model:
+
+* ``B[Q,p,q] ~ 0.05 N(0,1)``, symmetrised in ``pq``;
+* ``(pr|qs) = sum_Q B[Q,p,r] B[Q,q,s]`` and
+  ``<pq||rs> = (pr|qs) - (ps|qr)`` (antisymmetrised physicist notation,
+  occupied orbitals first, as ``mo_spin_eri`` returns them);
+* canonical Fock: occupied diagonal ~ U[-1.5,-0.3], virtual diagonal
+  ~ U[0.2,3.0], each sorted ascending (the reference's ``eigh`` denominators
+  are sorted, ``CCSD_Helper.py:327``), off-diagonal zero;
+* ``mu_z`` random symmetric with Frobenius norm 1 (x and y are zero).
+
+The draw order is fixed (B, occupied energies, virtual energies, mu_z) so a
+seed names a system on every platform (numpy's PCG64 streams are
+platform-independent).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class System:
+    o: int
+    v: int
+    nq: int
+    seed: int
+    B: np.ndarray          # (Q, n, n) float64
+    fock: np.ndarray       # (n, n) float64
+    mu: list = field(default_factory=list)   # [mu_x, mu_y, mu_z], each (n, n)
+
+    @property
+    def n(self) -> int:
+        return self.o + self.v
+
+    def tei(self) -> np.ndarray:
+        """Antisymmetrised <pq||rs> as an (n,n,n,n) float64 array (host)."""
+        return tei_from_df(self.B)
+
+    def eps(self) -> np.ndarray:
+        return np.diag(self.fock).copy()
+
+
+def synthetic_system(o: int, v: int, nq: int, seed: int) -> System:
+    rng = np.random.default_rng(seed)
+    n = o + v
+    B = rng.standard_normal((nq, n, n)) * 0.05
+    B = 0.5 * (B + B.transpose(0, 2, 1))
+    eo = np.sort(rng.uniform(-1.5, -0.3, o))
+    ev = np.sort(rng.uniform(0.2, 3.0, v))
+    M = rng.standard_normal((n, n))
+    M = 0.5 * (M + M.T)
+    mu_z = M / np.linalg.norm(M)
+    fock = np.diag(np.concatenate([eo, ev]))
+    zero = np.zeros((n, n))
+    return System(o=o, v=v, nq=nq, seed=seed, B=B, fock=fock, mu=[zero, zero.copy(), mu_z])
+
+
+def tei_from_df(B: np.ndarray) -> np.ndarray:
+    nq, n, _ = B.shape
+    Bm = B.reshape(nq, n * n)
+    # phys[p,q,r,s] = (pr|qs) = sum_Q B[Q,p,r] B[Q,q,s]
+    J = (Bm.T @ Bm).reshape(n, n, n, n)          # J[p,r,q,s]
+    phys = J.transpose(0, 2, 1, 3)               # [p,q,r,s]
+    return np.ascontiguousarray(phys - phys.transpose(0, 1, 3, 2))
+
+
+def mp2_guess(tei: np.ndarray, eps: np.ndarray, o: int) -> np.ndarray:
+    """t2 = <ij||ab> / (e_i + e_j - e_a - e_b) (``CCSD_Helper.py:102-124``)."""
+    eo, ev = eps[:o], eps[o:]
+    d = eo[:, None, None, None] + eo[None, :, None, None] - ev[None, None, :, None] - ev[None, None, None, :]
+    return tei[:o, :o, o:, o:] / d
+
+
+# Named workloads (sizes and generator parameters of the synthetic systems).
+WORKLOADS = {
+    "ccsd_o10_v14": dict(o=10, v=14, nq=72, seed=1014),
+    "ccsd_o10_v38": dict(o=10, v=38, nq=144, seed=1038),
+    "o8_v30": dict(o=8, v=30, nq=144, seed=830),
+    "o14_v58": dict(o=14, v=58, nq=144, seed=1458),
+    "o18_v82": dict(o=18, v=82, nq=144, seed=1882),
+    "o24_v160": dict(o=24, v=160, nq=480, seed=24160),
+    "o6_v12": dict(o=6, v=12, nq=72, seed=612),
+}
