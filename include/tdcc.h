@@ -1,0 +1,185 @@
+/*
+ * tdcc.h -- C ABI of libtdcc.so, the GB300 (sm_103a) engine for the
+ * time-dependent CCSD / CC2 hot path of yramis/python_code_to_check_C.
+ *
+ * The reference is pure Python (numpy + opt_einsum) and has no FFI; each
+ * entry point below names the reference method it replaces (file:line in the
+ * reference project).  A Python caller binds these with ctypes
+ * (python_code_to_check_c_gb300/_lib.py); any other host language binds the
+ * same symbols.
+ *
+ * Conventions
+ *  - Return value: TDCC_OK (0) or a negative TDCC_ERR_* code; the message of
+ *    the last failure on the calling thread is read with tdcc_last_error().
+ *  - Every array is caller-owned DEVICE memory, C-contiguous:
+ *      t1, l1 : complex128 [o][v]          (interleaved re, im doubles)
+ *      t2, l2 : complex128 [o][o][v][v]
+ *      F      : complex128 [n][n]          (Fock + field, n = o + v)
+ *      tei    : float64    [n][n][n][n]    antisymmetrised <pq||rs>,
+ *                                          occupied orbitals first
+ *      fock   : float64    [n][n]
+ *      mu     : float64    [n_mu][n][n]    dipole matrices (z is the last)
+ *  - `stream` is a cudaStream_t (0 = legacy default stream).  Calls are
+ *    asynchronous with respect to the host unless stated otherwise.
+ *  - A tdcc_system is not thread-safe: use one per host thread.
+ */
+#ifndef TDCC_H
+#define TDCC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tdcc_system_s* tdcc_system;
+
+enum {
+  TDCC_OK = 0,
+  TDCC_ERR_ARG = -1,       /* bad size / pointer / enum value              */
+  TDCC_ERR_CUDA = -2,      /* a CUDA runtime call failed                   */
+  TDCC_ERR_ALLOC = -3,     /* device allocation failed                     */
+  TDCC_ERR_STATE = -4,     /* call not valid in the current state          */
+  TDCC_ERR_NONFINITE = -5, /* propagation produced NaN/Inf                 */
+  TDCC_ERR_LIMIT = -6      /* size beyond a documented maximum             */
+};
+
+enum { TDCC_CCSD = 0, TDCC_CC2 = 1 };
+
+/* residual blocks */
+enum { TDCC_T1 = 0, TDCC_T2 = 1, TDCC_L1 = 2, TDCC_L2 = 3 };
+
+/* contraction arithmetic */
+enum {
+  TDCC_PREC_FP64 = 0,      /* every contraction in FP64 (the plain form)   */
+  TDCC_PREC_MIXED = 1      /* large contractions as split-BF16 tcgen05
+                              products, FP64 everywhere else               */
+};
+
+/* external field E(t); the Fock matrix seen by a stage at time t is
+   F(t) = fock - E(t) * mu_z  (mu_z = last dipole matrix).                 */
+enum {
+  TDCC_FIELD_NONE = 0,
+  TDCC_FIELD_SIN = 1,       /* E = A sin(w0 t)                              */
+  TDCC_FIELD_REFERENCE = 2, /* E = A exp(i 2 pi w0 t): the reference's Vt
+                               (CCSD_Helper.py:1197-1200)                  */
+  TDCC_FIELD_ENVELOPE = 3   /* E = A sin(w0 t) sum_k c_k exp(-(t-t_k)^2/(2 s^2)),
+                               t_k = env_t0 + k * env_dt                   */
+};
+
+#define TDCC_MAX_ENVELOPE 64
+
+typedef struct tdcc_field {
+  int kind;
+  double A;
+  double w0;
+  int n_env;                      /* number of envelope bumps (<= 64)       */
+  double env_t0, env_dt, env_sigma;
+  double env_c[TDCC_MAX_ENVELOPE];
+} tdcc_field;
+
+/* ABI version (increments on incompatible changes). */
+int tdcc_version(void);
+
+/* Copies the last error message of this thread into buf (NUL-terminated). */
+int tdcc_last_error(char* buf, size_t len);
+
+/* Number of kernels this library has launched in this process (all entry
+   points, all devices).  Used by benchmarks to report launch counts.      */
+long long tdcc_launch_count(void);
+
+/* Builds a system from device-resident integrals (replaces
+   CCSD_Helper.__init__ / TEI_MO / F_MO / Defd_dipole,
+   CCSD_Helper.py:26-54, 57-93, 970-980).  tei/fock/mu are borrowed: they
+   must stay valid until tdcc_system_destroy.  Allocates workspace lazily.  */
+int tdcc_system_create(int o, int v, const double* tei, const double* fock,
+                       const double* mu, int n_mu, tdcc_system* out);
+int tdcc_system_destroy(tdcc_system s);
+
+/* Selects the contraction arithmetic (TDCC_PREC_*) and, for the mixed mode,
+   the number of BF16 slices per operand (3..7).                           */
+int tdcc_set_precision(tdcc_system s, int mode, int slices);
+
+/* Bytes of device workspace currently held by the system.                 */
+long long tdcc_workspace_bytes(tdcc_system s);
+
+/* One right-hand side.  Replaces, by (method, block):
+     CCSD T1 : CCSD_Helper.T1eq_rhs      (CCSD_Helper.py:177-196)
+     CCSD T2 : CCSD_Helper.T2eq_rhs      (CCSD_Helper.py:268-309)
+     CCSD L1 : CCSD_Helper.lam_1eq_rhs   (CCSD_Helper.py:555-581)
+     CCSD L2 : CCSD_Helper.lam2eq_rhs    (CCSD_Helper.py:610-648)
+     CC2  T1 : CCSD_Helper.T1eq_rhs      (used by CC2, CC2_Helper.py:463)
+     CC2  T2 : CC2_Helper.T2eq_rhs_CC2   (CC2_Helper.py:12-47)
+     CC2  L1 : CC2_Helper.L1eq_rhs_CC2   (CC2_Helper.py:50-125)
+     CC2  L2 : CC2_Helper.L2eq_rhs_CC2   (CC2_Helper.py:128-175)
+   Inputs not used by a block may be NULL (T blocks ignore l1, l2).
+   `out` has the shape of the block's amplitude.                          */
+int tdcc_rhs(tdcc_system s, int method, int block, const void* t1, const void* t2,
+             const void* l1, const void* l2, const void* F, void* out, void* stream);
+
+/* Correlated one-particle density blocks and the dipole expectation value
+   sum_pq mu^k_pq rho_pq for every dipole component k (replaces
+   CCSD_Helper.dipole_moment, Dij/Dab/Dai, CCSD_Helper.py:984-1006,
+   1066-1092).  mu_out: device complex128[n_mu].                           */
+int tdcc_dipole(tdcc_system s, const void* t1, const void* t2, const void* l1,
+                const void* l2, void* mu_out, void* stream);
+
+/* One step of the block-frozen RK4 propagator (the loop body of
+   CCSD_Helper.Runge_Kutta_solver, CCSD_Helper.py:1206-1240, and of
+   CC2_Helper.Runge_Kutta_solver_CC2, CC2_Helper.py:451-472, with
+   ft1/ft2/fL1/fL2 at CCSD_Helper.py:1158-1187 and CC2_Helper.py:412-433).
+   t_prev is the time before the step; the stages see the field at
+   t = t_prev + dt, t + dt/2, t + dt (the reference advances t first).
+   The new state round(old, precs) + delta is written to the *_out arrays
+   (which may alias the inputs).  If mu_out is not NULL the dipole of the
+   new state is written there (complex128[n_mu]).                          */
+int tdcc_rk4_step(tdcc_system s, int method, const void* t1, const void* t2,
+                  const void* l1, const void* l2, void* t1_out, void* t2_out,
+                  void* l1_out, void* l2_out, double t_prev, double dt, int precs,
+                  const tdcc_field* field, void* mu_out, void* stream);
+
+/* nsteps RK4 steps with the state resident on the device and the step
+   captured once in a CUDA graph.  The state arrays are read at entry and
+   overwritten with the final state.  mu_traj (device complex128[nsteps])
+   receives mu_z after every step.  Synchronous: returns after the last
+   step completed (TDCC_ERR_NONFINITE if the final state is not finite).   */
+int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void* l2,
+                   double t0, double dt, int nsteps, int precs,
+                   const tdcc_field* field, void* mu_traj, void* stream);
+
+/* Writes a JSON description of the op list that computes (method, block)
+   for sizes (o, v): buffer slots, and per op the GEMM mode groups / strides
+   or the elementwise terms, plus whether the op runs once per RK4 step or
+   in every stage.  block = 4 selects the density / dipole program.  Needs no
+   GPU (used by the CPU tests to check the programs; no counterpart in the
+   reference).  Returns the JSON length; TDCC_ERR_LIMIT if buf is too small.*/
+long long tdcc_program_json(int o, int v, int method, int block, int n_mu, char* buf,
+                            size_t len);
+
+/* Per-kernel timing record of tdcc_profile_step. */
+typedef struct tdcc_op_record {
+  char tag[96];   /* "<program>:<einsum>" or the kernel's role               */
+  int kind;       /* 0 contraction, 1 elementwise, 2 trace, 3 RK4 / field    */
+  int block;      /* 0..3 = T1, T2, L1, L2 block; 4 = density; 5 = step      */
+  int stage;      /* 0 = prologue (once per step), 1..4 = RK4 stage          */
+  int backend;    /* contractions: 0 FP64 CUDA cores, 1 tensor cores         */
+  double flops;   /* real floating-point operations of the op               */
+  double bytes;   /* compulsory bytes read + written by the op              */
+  double ms;      /* device time from CUDA events on the launching stream    */
+} tdcc_op_record;
+
+/* Runs one RK4 step eagerly on a single stream with a CUDA-event pair around
+   every kernel and returns one record per launch (diagnostics and the
+   benchmark's roofline figures; no counterpart in the reference).  The state
+   is not modified.  Synchronous.                                          */
+int tdcc_profile_step(tdcc_system s, int method, const void* t1, const void* t2,
+                      const void* l1, const void* l2, double t_prev, double dt,
+                      int precs, const tdcc_field* field, tdcc_op_record* recs,
+                      int max_recs, int* n_recs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDCC_H */

@@ -1,0 +1,673 @@
+// extern "C" entry points of libtdcc.so (declared in include/tdcc.h).
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tdcc.h"
+#include "engine.h"
+#include "rk4.h"
+
+namespace tdcc {
+
+static thread_local std::string g_err;
+void set_error(const std::string& m) { g_err = m; }
+
+void build_t1(Program& p);
+void build_t2_ccsd(Program& p);
+void build_t2_cc2(Program& p);
+void build_l1_ccsd(Program& p);
+void build_l2_ccsd(Program& p);
+void build_l1_cc2(Program& p);
+void build_l2_cc2(Program& p, const View& ones_v);
+void build_density(Program& p, int n_mu);
+
+// Tensor-core backend hooks (gemm_tc.cu); FP64 only when not compiled in.
+bool tc_available();
+
+struct ProgInst {
+  std::unique_ptr<Program> prog;
+  std::vector<void*> bases;
+};
+
+}  // namespace tdcc
+
+using namespace tdcc;
+
+struct tdcc_system_s {
+  Dims dims;
+  const double* tei = nullptr;
+  const double* fock = nullptr;
+  const double* mu = nullptr;
+  int n_mu = 0;
+  int prec_mode = TDCC_PREC_FP64;
+  int slices = 5;
+  int device = 0;
+  std::unique_ptr<ProgInst> rhs[2][4];
+  std::unique_ptr<ProgInst> dens;
+  std::vector<void*> owned;
+  long long ws_bytes = 0;
+
+  // RK4 machinery
+  bool rk_ready = false;
+  StepCtx* ctx = nullptr;          // device
+  double2* Fs = nullptr;           // 3 x n x n dressed Fock matrices
+  double2* kbuf[4] = {};
+  double2* acc[4] = {};
+  double2* yin[4] = {};
+  double2* st[2][4] = {};          // ping-pong state buffers
+  double2* res = nullptr;          // dipole components
+  cudaStream_t main = nullptr;
+  cudaStream_t bs[4] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[4] = {}, ev_user = nullptr;
+  // captured step graphs (A->B, B->A)
+  cudaGraphExec_t gexec[2] = {};
+  int g_method = -1, g_precs = -999, g_prec_mode = -1;
+  double g_dt = 0.0;
+  double2* g_traj = nullptr;
+  long long g_nodes[2] = {0, 0};   // kernel nodes per captured step graph
+
+  long long nel(int b) const {
+    const long long o = dims.o, v = dims.v;
+    return (b == TDCC_T1 || b == TDCC_L1) ? o * v : o * o * v * v;
+  }
+};
+
+namespace {
+
+#define CK(x)                                                                      \
+  do {                                                                             \
+    cudaError_t e__ = (x);                                                         \
+    if (e__ != cudaSuccess) {                                                      \
+      throw std::runtime_error(std::string(#x) + ": " + cudaGetErrorString(e__)); \
+    }                                                                              \
+  } while (0)
+
+void* dalloc(tdcc_system s, size_t bytes) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    throw std::runtime_error("cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+  }
+  s->owned.push_back(p);
+  s->ws_bytes += (long long)bytes;
+  return p;
+}
+
+void bind_fixed(tdcc_system s, std::vector<void*>& b) {
+  b[S_TEI] = const_cast<double*>(s->tei);
+  b[S_MU] = const_cast<double*>(s->mu);
+}
+
+ProgInst& get_rhs(tdcc_system s, int method, int block) {
+  auto& slot = s->rhs[method][block];
+  if (slot) return *slot;
+  auto pi = std::make_unique<ProgInst>();
+  static const char* names[2][4] = {{"ccsd_t1", "ccsd_t2", "ccsd_l1", "ccsd_l2"},
+                                    {"cc2_t1", "cc2_t2", "cc2_l1", "cc2_l2"}};
+  pi->prog = std::make_unique<Program>(s->dims, names[method][block]);
+  Program& p = *pi->prog;
+  if (block == TDCC_T1)
+    build_t1(p);
+  else if (method == TDCC_CCSD && block == TDCC_T2)
+    build_t2_ccsd(p);
+  else if (method == TDCC_CCSD && block == TDCC_L1)
+    build_l1_ccsd(p);
+  else if (method == TDCC_CCSD && block == TDCC_L2)
+    build_l2_ccsd(p);
+  else if (block == TDCC_T2)
+    build_t2_cc2(p);
+  else if (block == TDCC_L1)
+    build_l1_cc2(p);
+  else
+    build_l2_cc2(p, p.ones("ones_v", s->dims.v));
+  // the block's own amplitude and the dressed Fock vary across RK4 stages
+  p.analyse({S_T1 + block, S_F});
+  p.select_backend(s->prec_mode, 1LL << 40);
+  pi->bases.assign(p.slots.size(), nullptr);
+  s->ws_bytes += p.allocate(pi->bases, s->owned);
+  bind_fixed(s, pi->bases);
+  slot = std::move(pi);
+  return *slot;
+}
+
+ProgInst& get_density(tdcc_system s) {
+  if (s->dens) return *s->dens;
+  auto pi = std::make_unique<ProgInst>();
+  pi->prog = std::make_unique<Program>(s->dims, "density");
+  build_density(*pi->prog, s->n_mu);
+  pi->prog->analyse({});
+  pi->bases.assign(pi->prog->slots.size(), nullptr);
+  s->ws_bytes += pi->prog->allocate(pi->bases, s->owned);
+  bind_fixed(s, pi->bases);
+  s->dens = std::move(pi);
+  return *s->dens;
+}
+
+void ensure_rk(tdcc_system s) {
+  if (s->rk_ready) return;
+  const long long n = s->dims.n;
+  s->ctx = static_cast<StepCtx*>(dalloc(s, sizeof(StepCtx)));
+  s->Fs = static_cast<double2*>(dalloc(s, 3 * n * n * sizeof(double2)));
+  for (int b = 0; b < 4; ++b) {
+    const size_t bytes = s->nel(b) * sizeof(double2);
+    s->kbuf[b] = static_cast<double2*>(dalloc(s, bytes));
+    s->acc[b] = static_cast<double2*>(dalloc(s, bytes));
+    s->yin[b] = static_cast<double2*>(dalloc(s, bytes));
+    s->st[0][b] = static_cast<double2*>(dalloc(s, bytes));
+    s->st[1][b] = static_cast<double2*>(dalloc(s, bytes));
+  }
+  s->res = static_cast<double2*>(dalloc(s, 4 * sizeof(double2)));
+  CK(cudaStreamCreateWithFlags(&s->main, cudaStreamNonBlocking));
+  for (int b = 0; b < 4; ++b) {
+    CK(cudaStreamCreateWithFlags(&s->bs[b], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&s->ev_join[b], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&s->ev_user, cudaEventDisableTiming));
+  s->rk_ready = true;
+}
+
+// Optional per-launch timing (tdcc_profile_step).
+struct Prof {
+  struct Rec {
+    std::string tag;
+    int kind, block, stage, backend;
+    double flops, bytes;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> recs;
+  void add_prog(const std::vector<Program::Timed>& tm, int block, int stage) {
+    for (const auto& t : tm) {
+      const Op& op = *t.op;
+      const int kind = op.kind == OP_GEMM ? 0 : op.kind == OP_ADD ? 1 : 2;
+      recs.push_back({op.tag, kind, block, stage, op.backend, (double)op.flops, (double)op.bytes, t.a, t.b});
+    }
+  }
+};
+
+template <class F>
+void timed_launch(Prof* pf, cudaStream_t st, const char* tag, int block, int stage, double bytes, F&& fn) {
+  if (!pf) {
+    CK(fn());
+    return;
+  }
+  Prof::Rec r{tag, 3, block, stage, 0, 0.0, bytes, nullptr, nullptr};
+  cudaEventCreate(&r.a);
+  cudaEventCreate(&r.b);
+  cudaEventRecord(r.a, st);
+  CK(fn());
+  cudaEventRecord(r.b, st);
+  pf->recs.push_back(r);
+}
+
+// One RK4 block (ft1/ft2/fL1/fL2): prologue once, four stages, final update.
+void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* out_b, double dt,
+               int precs, cudaStream_t st, Prof* pf = nullptr) {
+  ProgInst& pi = get_rhs(s, method, b);
+  Program& p = *pi.prog;
+  auto& B = pi.bases;
+  for (int k = 0; k < 4; ++k) B[S_T1 + k] = in[k];
+  B[S_OUT] = s->kbuf[b];
+  const long long n = s->nel(b);
+  const long long nn = (long long)s->dims.n * s->dims.n;
+  std::vector<Program::Timed> tm;
+  B[S_F] = s->Fs;
+  CK(p.run(B, st, Program::PROLOGUE, pf ? &tm : nullptr));
+  if (pf) pf->add_prog(tm, b, 0);
+  for (int stage = 1; stage <= 4; ++stage) {
+    B[S_T1 + b] = stage == 1 ? in[b] : s->yin[b];
+    B[S_F] = s->Fs + (stage == 1 ? 0 : stage < 4 ? 1 : 2) * nn;
+    tm.clear();
+    CK(p.run(B, st, Program::STAGE, pf ? &tm : nullptr));
+    if (pf) pf->add_prog(tm, b, stage);
+    const double h = stage < 3 ? dt / 2.0 : dt;
+    timed_launch(pf, st, "rk4_stage_axpy", b, stage, (double)n * 16 * (stage == 1 ? 3 : stage == 4 ? 3 : 5),
+                 [&] { return launch_rk4_stage(in[b], s->kbuf[b], s->acc[b], s->yin[b], n, stage, h, st); });
+  }
+  const int sign = (b == TDCC_T1 || b == TDCC_T2) ? -1 : +1;
+  const double scale = precs >= 0 ? std::pow(10.0, (double)precs) : 1.0;
+  timed_launch(pf, st, "rk4_round_update", b, 4, (double)n * 16 * 3, [&] {
+    return launch_rk4_finish(in[b], s->acc[b], out_b, n, dt / 6.0, sign, scale, precs >= 0 ? 1 : 0, st);
+  });
+}
+
+// Full step on s->main: field, dressing, 4 concurrent blocks, dipole of the
+// new state.  `in` and `out` must not alias.  With a profiler everything
+// runs serially on s->main.
+void run_step(tdcc_system s, int method, double2* const in[4], double2* const out[4], double dt,
+              int precs, double2* traj, Prof* pf = nullptr) {
+  cudaStream_t m = s->main;
+  const long long nn = (long long)s->dims.n * s->dims.n;
+  timed_launch(pf, m, "advance_field", 5, 0, 0.0, [&] { return launch_advance_field(s->ctx, m); });
+  const double* muz = s->mu + (long long)(s->n_mu - 1) * nn;
+  timed_launch(pf, m, "dress_fock", 5, 0, (double)nn * (8 + 8 + 3 * 16),
+               [&] { return launch_dress(s->ctx, s->fock, muz, s->Fs, s->dims.n, m); });
+  if (pf) {
+    for (int b = 0; b < 4; ++b) run_block(s, method, b, in, out[b], dt, precs, m, pf);
+  } else {
+    CK(cudaEventRecord(s->ev_fork, m));
+    for (int b = 0; b < 4; ++b) {
+      CK(cudaStreamWaitEvent(s->bs[b], s->ev_fork, 0));
+      run_block(s, method, b, in, out[b], dt, precs, s->bs[b]);
+      CK(cudaEventRecord(s->ev_join[b], s->bs[b]));
+    }
+    for (int b = 0; b < 4; ++b) CK(cudaStreamWaitEvent(m, s->ev_join[b], 0));
+  }
+  ProgInst& d = get_density(s);
+  for (int k = 0; k < 4; ++k) d.bases[S_T1 + k] = out[k];
+  d.bases[S_RES] = s->res;
+  std::vector<Program::Timed> tm;
+  CK(d.prog->run(d.bases, m, Program::ALL, pf ? &tm : nullptr));
+  if (pf) pf->add_prog(tm, 4, 0);
+  timed_launch(pf, m, "record_mu", 5, 0, 0.0,
+               [&] { return launch_record_mu(s->ctx, s->res, s->n_mu, traj, nullptr, m); });
+}
+
+void set_ctx(tdcc_system s, double t, double dt, const tdcc_field* f, cudaStream_t st) {
+  StepCtx h;
+  memset(&h, 0, sizeof(h));
+  h.t = t;
+  h.dt = dt;
+  if (f) h.field = *f;
+  h.step = 0;
+  CK(cudaMemcpyAsync(s->ctx, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
+}
+
+int fail(int code, const std::string& m) {
+  set_error(m);
+  return code;
+}
+
+bool valid_method(int m) { return m == TDCC_CCSD || m == TDCC_CC2; }
+
+}  // namespace
+
+extern "C" {
+
+int tdcc_version(void) { return 1; }
+
+int tdcc_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return TDCC_ERR_ARG;
+  strncpy(buf, g_err.c_str(), len - 1);
+  buf[len - 1] = '\0';
+  return TDCC_OK;
+}
+
+long long tdcc_launch_count(void) { return launch_count(); }
+
+int tdcc_system_create(int o, int v, const double* tei, const double* fock, const double* mu,
+                       int n_mu, tdcc_system* out) {
+  if (!out) return fail(TDCC_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (o < 1 || v < 1) return fail(TDCC_ERR_ARG, "o and v must be >= 1");
+  if ((long long)(o + v) * (o + v) * (o + v) * (o + v) >= (1LL << 40))
+    return fail(TDCC_ERR_LIMIT, "n^4 too large");
+  if (!tei || !fock || !mu) return fail(TDCC_ERR_ARG, "tei/fock/mu must be device pointers");
+  if (n_mu < 1 || n_mu > 3) return fail(TDCC_ERR_ARG, "n_mu must be 1..3");
+  auto* s = new tdcc_system_s;
+  s->dims = Dims{o, v, o + v};
+  s->tei = tei;
+  s->fock = fock;
+  s->mu = mu;
+  s->n_mu = n_mu;
+  cudaGetDevice(&s->device);
+  *out = s;
+  return TDCC_OK;
+}
+
+int tdcc_system_destroy(tdcc_system s) {
+  if (!s) return TDCC_OK;
+  cudaDeviceSynchronize();
+  for (auto& g : s->gexec)
+    if (g) cudaGraphExecDestroy(g);
+  if (s->rk_ready) {
+    cudaStreamDestroy(s->main);
+    for (int b = 0; b < 4; ++b) {
+      cudaStreamDestroy(s->bs[b]);
+      cudaEventDestroy(s->ev_join[b]);
+    }
+    cudaEventDestroy(s->ev_fork);
+    cudaEventDestroy(s->ev_user);
+  }
+  for (void* p : s->owned) cudaFree(p);
+  delete s;
+  return TDCC_OK;
+}
+
+int tdcc_set_precision(tdcc_system s, int mode, int slices) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (mode != TDCC_PREC_FP64 && mode != TDCC_PREC_MIXED) return fail(TDCC_ERR_ARG, "bad precision mode");
+  if (mode == TDCC_PREC_MIXED && !tc_available())
+    return fail(TDCC_ERR_STATE, "tensor-core backend not built into this library");
+  if (mode == TDCC_PREC_MIXED && (slices < 3 || slices > 7)) return fail(TDCC_ERR_ARG, "slices must be 3..7");
+  s->prec_mode = mode;
+  s->slices = slices;
+  for (auto& mrow : s->rhs)
+    for (auto& pi : mrow)
+      if (pi) pi->prog->select_backend(mode, 1LL << 40);
+  return TDCC_OK;
+}
+
+long long tdcc_workspace_bytes(tdcc_system s) { return s ? s->ws_bytes : 0; }
+
+int tdcc_rhs(tdcc_system s, int method, int block, const void* t1, const void* t2, const void* l1,
+             const void* l2, const void* F, void* out, void* stream) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
+  if (block < 0 || block > 3) return fail(TDCC_ERR_ARG, "bad block");
+  if (!t1 || !t2 || !F || !out) return fail(TDCC_ERR_ARG, "t1/t2/F/out must not be NULL");
+  if (block >= TDCC_L1 && (!l1 || !l2)) return fail(TDCC_ERR_ARG, "Lambda blocks need l1 and l2");
+  try {
+    ProgInst& pi = get_rhs(s, method, block);
+    auto& B = pi.bases;
+    B[S_T1] = const_cast<void*>(t1);
+    B[S_T2] = const_cast<void*>(t2);
+    B[S_L1] = const_cast<void*>(l1);
+    B[S_L2] = const_cast<void*>(l2);
+    B[S_F] = const_cast<void*>(F);
+    B[S_OUT] = out;
+    cudaError_t e = pi.prog->run(B, static_cast<cudaStream_t>(stream), Program::ALL);
+    if (e != cudaSuccess) return TDCC_ERR_CUDA;
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  return TDCC_OK;
+}
+
+int tdcc_dipole(tdcc_system s, const void* t1, const void* t2, const void* l1, const void* l2,
+                void* mu_out, void* stream) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!t1 || !t2 || !l1 || !l2 || !mu_out) return fail(TDCC_ERR_ARG, "NULL argument");
+  try {
+    ProgInst& d = get_density(s);
+    d.bases[S_T1] = const_cast<void*>(t1);
+    d.bases[S_T2] = const_cast<void*>(t2);
+    d.bases[S_L1] = const_cast<void*>(l1);
+    d.bases[S_L2] = const_cast<void*>(l2);
+    d.bases[S_RES] = mu_out;
+    if (d.prog->run(d.bases, static_cast<cudaStream_t>(stream), Program::ALL) != cudaSuccess)
+      return TDCC_ERR_CUDA;
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  return TDCC_OK;
+}
+
+int tdcc_rk4_step(tdcc_system s, int method, const void* t1, const void* t2, const void* l1,
+                  const void* l2, void* t1_out, void* t2_out, void* l1_out, void* l2_out,
+                  double t_prev, double dt, int precs, const tdcc_field* field, void* mu_out,
+                  void* stream) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
+  if (!t1 || !t2 || !l1 || !l2 || !t1_out || !t2_out || !l1_out || !l2_out)
+    return fail(TDCC_ERR_ARG, "NULL state pointer");
+  if (!(dt > 0.0)) return fail(TDCC_ERR_ARG, "dt must be > 0");
+  if (precs > 22) return fail(TDCC_ERR_ARG, "precs must be <= 22 (negative: no rounding)");
+  try {
+    ensure_rk(s);
+    cudaStream_t user = static_cast<cudaStream_t>(stream);
+    CK(cudaEventRecord(s->ev_user, user));
+    CK(cudaStreamWaitEvent(s->main, s->ev_user, 0));
+    set_ctx(s, t_prev, dt, field, s->main);
+    double2* in[4] = {(double2*)t1, (double2*)t2, (double2*)l1, (double2*)l2};
+    double2* tmp[4] = {s->st[1][0], s->st[1][1], s->st[1][2], s->st[1][3]};
+    run_step(s, method, in, tmp, dt, precs, nullptr);
+    void* outs[4] = {t1_out, t2_out, l1_out, l2_out};
+    for (int b = 0; b < 4; ++b)
+      CK(cudaMemcpyAsync(outs[b], tmp[b], s->nel(b) * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
+    if (mu_out) CK(cudaMemcpyAsync(mu_out, s->res, s->n_mu * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
+    CK(cudaEventRecord(s->ev_user, s->main));
+    CK(cudaStreamWaitEvent(user, s->ev_user, 0));
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  return TDCC_OK;
+}
+
+int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void* l2, double t0,
+                   double dt, int nsteps, int precs, const tdcc_field* field, void* mu_traj,
+                   void* stream) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
+  if (!t1 || !t2 || !l1 || !l2 || !mu_traj) return fail(TDCC_ERR_ARG, "NULL argument");
+  if (nsteps < 0) return fail(TDCC_ERR_ARG, "nsteps < 0");
+  if (!(dt > 0.0)) return fail(TDCC_ERR_ARG, "dt must be > 0");
+  if (precs > 22) return fail(TDCC_ERR_ARG, "precs must be <= 22");
+  try {
+    ensure_rk(s);
+    cudaStream_t user = static_cast<cudaStream_t>(stream);
+    CK(cudaEventRecord(s->ev_user, user));
+    CK(cudaStreamWaitEvent(s->main, s->ev_user, 0));
+    void* st_user[4] = {t1, t2, l1, l2};
+    for (int b = 0; b < 4; ++b)
+      CK(cudaMemcpyAsync(s->st[0][b], st_user[b], s->nel(b) * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
+    set_ctx(s, t0, dt, field, s->main);
+    // (re)capture the two ping-pong step graphs when the configuration changed
+    if (s->g_method != method || s->g_dt != dt || s->g_precs != precs || s->g_prec_mode != s->prec_mode ||
+        s->g_traj != mu_traj || !s->gexec[0]) {
+      for (auto& g : s->gexec)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+      // build programs (allocations) before capture
+      for (int b = 0; b < 4; ++b) get_rhs(s, method, b);
+      get_density(s);
+      const long long before_capture = launch_count();
+      for (int k = 0; k < 2; ++k) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(s->main, cudaStreamCaptureModeThreadLocal));
+        try {
+          run_step(s, method, s->st[k], s->st[1 - k], dt, precs, (double2*)mu_traj);
+        } catch (...) {
+          cudaStreamEndCapture(s->main, &graph);
+          throw;
+        }
+        CK(cudaStreamEndCapture(s->main, &graph));
+        size_t nn = 0;
+        CK(cudaGraphGetNodes(graph, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        CK(cudaGraphGetNodes(graph, nodes.data(), &nn));
+        long long kn = 0;
+        for (auto nd : nodes) {
+          cudaGraphNodeType ty;
+          CK(cudaGraphNodeGetType(nd, &ty));
+          if (ty == cudaGraphNodeTypeKernel) ++kn;
+        }
+        s->g_nodes[k] = kn;
+        CK(cudaGraphInstantiate(&s->gexec[k], graph, 0));
+        cudaGraphDestroy(graph);
+      }
+      count_launch(before_capture - launch_count());  // captured, not executed
+      s->g_method = method;
+      s->g_dt = dt;
+      s->g_precs = precs;
+      s->g_prec_mode = s->prec_mode;
+      s->g_traj = (double2*)mu_traj;
+    }
+    // the step graphs run on the caller's stream, so its events bracket them
+    CK(cudaEventRecord(s->ev_user, s->main));
+    CK(cudaStreamWaitEvent(user, s->ev_user, 0));
+    for (int i = 0; i < nsteps; ++i) {
+      CK(cudaGraphLaunch(s->gexec[i & 1], user));
+      count_launch(s->g_nodes[i & 1]);
+    }
+    const int fin = nsteps & 1;
+    for (int b = 0; b < 4; ++b)
+      CK(cudaMemcpyAsync(st_user[b], s->st[fin][b], s->nel(b) * sizeof(double2), cudaMemcpyDeviceToDevice, user));
+    CK(cudaStreamSynchronize(user));
+    if (nsteps > 0) {
+      double2 last;
+      CK(cudaMemcpy(&last, (double2*)mu_traj + (nsteps - 1), sizeof(last), cudaMemcpyDeviceToHost));
+      if (!std::isfinite(last.x) || !std::isfinite(last.y))
+        return fail(TDCC_ERR_NONFINITE, "dipole is not finite after propagation");
+    }
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  return TDCC_OK;
+}
+
+int tdcc_profile_step(tdcc_system s, int method, const void* t1, const void* t2, const void* l1,
+                      const void* l2, double t_prev, double dt, int precs, const tdcc_field* field,
+                      tdcc_op_record* recs, int max_recs, int* n_recs) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
+  if (!t1 || !t2 || !l1 || !l2 || !recs || !n_recs || max_recs < 0) return fail(TDCC_ERR_ARG, "NULL argument");
+  if (!(dt > 0.0)) return fail(TDCC_ERR_ARG, "dt must be > 0");
+  Prof pf;
+  try {
+    ensure_rk(s);
+    CK(cudaDeviceSynchronize());
+    set_ctx(s, t_prev, dt, field, s->main);
+    double2* in[4] = {(double2*)t1, (double2*)t2, (double2*)l1, (double2*)l2};
+    double2* tmp[4] = {s->st[1][0], s->st[1][1], s->st[1][2], s->st[1][3]};
+    run_step(s, method, in, tmp, dt, precs, nullptr, &pf);
+    CK(cudaStreamSynchronize(s->main));
+  } catch (const std::exception& ex) {
+    for (auto& r : pf.recs) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  int k = 0;
+  for (auto& r : pf.recs) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    if (k < max_recs) {
+      tdcc_op_record& o = recs[k];
+      memset(&o, 0, sizeof(o));
+      strncpy(o.tag, r.tag.c_str(), sizeof(o.tag) - 1);
+      o.kind = r.kind;
+      o.block = r.block;
+      o.stage = r.stage;
+      o.backend = r.backend;
+      o.flops = r.flops;
+      o.bytes = r.bytes;
+      o.ms = ms;
+    }
+    ++k;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  *n_recs = k;
+  return TDCC_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// program introspection (no GPU needed)
+// ---------------------------------------------------------------------------
+namespace {
+
+void build_program(Program& p, int method, int block, int n_mu) {
+  if (block == 4)
+    build_density(p, n_mu);
+  else if (block == TDCC_T1)
+    build_t1(p);
+  else if (method == TDCC_CCSD && block == TDCC_T2)
+    build_t2_ccsd(p);
+  else if (method == TDCC_CCSD && block == TDCC_L1)
+    build_l1_ccsd(p);
+  else if (method == TDCC_CCSD && block == TDCC_L2)
+    build_l2_ccsd(p);
+  else if (block == TDCC_T2)
+    build_t2_cc2(p);
+  else if (block == TDCC_L1)
+    build_l1_cc2(p);
+  else
+    build_l2_cc2(p, p.ones("ones_v", p.dims.v));
+  if (block == 4)
+    p.analyse({});
+  else
+    p.analyse({S_T1 + block, S_F});
+}
+
+std::string jarr(const long long* x, int n) {
+  std::string s = "[";
+  for (int i = 0; i < n; ++i) s += (i ? "," : "") + std::to_string(x[i]);
+  return s + "]";
+}
+std::string jarr(const int* x, int n) {
+  std::string s = "[";
+  for (int i = 0; i < n; ++i) s += (i ? "," : "") + std::to_string(x[i]);
+  return s + "]";
+}
+std::string jnum(double x) {
+  char b[64];
+  snprintf(b, sizeof(b), "%.17g", x);
+  return b;
+}
+std::string jgroup(const ModeGroup& g) {
+  return "{\"n\":" + std::to_string(g.n) + ",\"dim\":" + jarr(g.dim, g.n) + ",\"s0\":" + jarr(g.s0, g.n) +
+         ",\"s1\":" + jarr(g.s1, g.n) + "}";
+}
+
+std::string program_json(const Program& p) {
+  std::string j = "{\"name\":\"" + p.name + "\",\"slots\":[";
+  for (size_t i = 0; i < p.slots.size(); ++i) {
+    const auto& s = p.slots[i];
+    j += (i ? "," : "") + std::string("{\"name\":\"") + s.name + "\",\"dt\":" + std::to_string(s.dt) +
+         ",\"numel\":" + std::to_string(s.numel) + ",\"fixed\":" + (s.fixed ? "true" : "false") +
+         ",\"ones\":" + (s.init.empty() ? "false" : "true") + "}";
+  }
+  j += "],\"ops\":[";
+  for (size_t i = 0; i < p.ops.size(); ++i) {
+    const Op& op = p.ops[i];
+    j += i ? "," : "";
+    const std::string var = op.varying ? "true" : "false";
+    if (op.kind == OP_GEMM) {
+      const GemmArgs& g = op.g;
+      j += "{\"kind\":\"gemm\",\"tag\":\"" + op.tag + "\",\"varying\":" + var +
+           ",\"sa\":" + std::to_string(op.sa) + ",\"oa\":" + std::to_string(op.oa) + ",\"dta\":" + std::to_string(op.dta) +
+           ",\"sb\":" + std::to_string(op.sb) + ",\"ob\":" + std::to_string(op.ob) + ",\"dtb\":" + std::to_string(op.dtb) +
+           ",\"sc\":" + std::to_string(op.sc) + ",\"oc\":" + std::to_string(op.oc) + ",\"dtc\":" + std::to_string(op.dtc) +
+           ",\"M\":" + std::to_string(g.M) + ",\"N\":" + std::to_string(g.N) + ",\"K\":" + std::to_string(g.K) +
+           ",\"gm\":" + jgroup(g.gm) + ",\"gn\":" + jgroup(g.gn) + ",\"gk\":" + jgroup(g.gk) +
+           ",\"ar\":" + jnum(g.ar) + ",\"ai\":" + jnum(g.ai) + ",\"acc\":" + std::to_string(g.acc) +
+           ",\"atomic\":" + std::to_string(g.atomic) + ",\"flops\":" + std::to_string(op.flops) + "}";
+    } else if (op.kind == OP_ADD) {
+      const AddArgs& a = op.a;
+      j += "{\"kind\":\"add\",\"varying\":" + var + ",\"sc\":" + std::to_string(op.add_sc) +
+           ",\"oc\":" + std::to_string(op.add_oc) + ",\"cc\":" + std::to_string(a.cc) +
+           ",\"acc\":" + std::to_string(a.acc) + ",\"d\":" + jarr(a.d, 4) + ",\"sC\":" + jarr(a.sC, 4) + ",\"terms\":[";
+      for (int t = 0; t < a.nt; ++t) {
+        const AddTerm& T = a.t[t];
+        j += (t ? "," : "") + std::string("{\"sa\":") + std::to_string(op.add_slots[t][0]) +
+             ",\"oa\":" + std::to_string(op.add_off[t][0]) + ",\"ac\":" + std::to_string(T.ac) +
+             ",\"sA\":" + jarr(T.sA, 4) + ",\"sb\":" + std::to_string(op.add_slots[t][1]) +
+             ",\"ob\":" + std::to_string(op.add_off[t][1]) + ",\"bc\":" + std::to_string(T.bc) +
+             ",\"sB\":" + jarr(T.sB, 4) + ",\"cr\":" + jnum(T.cr) + ",\"ci\":" + jnum(T.ci) + "}";
+      }
+      j += "]}";
+    } else {
+      j += "{\"kind\":\"trace\",\"varying\":" + var + ",\"slots\":" + jarr(op.tr_slots, 4) +
+           ",\"n_mu\":" + std::to_string(op.tr_n_mu) + "}";
+    }
+  }
+  return j + "]}";
+}
+
+}  // namespace
+
+extern "C" long long tdcc_program_json(int o, int v, int method, int block, int n_mu, char* buf,
+                                       size_t len) {
+  if (o < 1 || v < 1 || !valid_method(method) || block < 0 || block > 4 || n_mu < 1 || n_mu > 3)
+    return fail(TDCC_ERR_ARG, "bad arguments");
+  try {
+    Program p(Dims{o, v, o + v}, "introspect");
+    build_program(p, method, block, n_mu);
+    const std::string j = program_json(p);
+    if (!buf || len < j.size() + 1) return fail(TDCC_ERR_LIMIT, "buffer too small: need " + std::to_string(j.size() + 1));
+    memcpy(buf, j.c_str(), j.size() + 1);
+    return (long long)j.size();
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_ARG, ex.what());
+  }
+}

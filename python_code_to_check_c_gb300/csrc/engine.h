@@ -1,0 +1,223 @@
+// Internal engine of libtdcc.so: strided tensor views, the contraction /
+// elementwise op records, and "programs" (ordered op lists with symbolic
+// buffer slots) that the residual builders emit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace tdcc {
+
+enum DType : int { R64 = 0, C64 = 1 };
+
+// ---------------------------------------------------------------------------
+// Kernel argument blocks (passed by value to the kernels)
+// ---------------------------------------------------------------------------
+constexpr int kMaxModes = 3;
+
+// A group of tensor modes flattened into one GEMM dimension.  s0/s1 are the
+// element strides of each mode in the two tensors that carry the group
+// (M: A and C, N: B and C, K: A and B).  The last mode varies fastest.
+struct ModeGroup {
+  int n;
+  int dim[kMaxModes];
+  long long s0[kMaxModes];
+  long long s1[kMaxModes];
+};
+
+struct GemmArgs {
+  const void* A;
+  const void* B;
+  void* C;
+  int M, N, K;
+  ModeGroup gm, gn, gk;
+  double ar, ai;   // alpha
+  int acc;         // C += alpha*AB (else C = alpha*AB)
+  int kchunk;      // K range per blockIdx.z
+  int atomic;      // split-K: accumulate with atomics (C pre-initialised)
+};
+
+constexpr int kMaxAddTerms = 6;
+
+struct AddTerm {
+  const void* A;   // never null
+  const void* B;   // optional second factor (elementwise product), may be null
+  long long sA[4];
+  long long sB[4];
+  int ac, bc;      // A / B complex?
+  double cr, ci;   // coefficient
+};
+
+struct AddArgs {
+  void* C;
+  long long sC[4];
+  int d[4];
+  long long total;
+  int cc;          // C complex?
+  int acc;         // C += sum (else C = sum)
+  int nt;
+  AddTerm t[kMaxAddTerms];
+};
+
+// ---------------------------------------------------------------------------
+// Views and programs
+// ---------------------------------------------------------------------------
+// Fixed slots bound by the caller of a program at run time.
+enum Slot : int {
+  S_TEI = 0,   // R64 [n,n,n,n]
+  S_F,         // C64 [n,n]  dressed Fock of the stage
+  S_T1, S_T2, S_L1, S_L2,  // C64 amplitudes
+  S_OUT,       // C64 residual output
+  S_MU,        // R64 [n_mu,n,n]
+  S_RES,       // C64 small result vector (dipole components)
+  kNumFixedSlots
+};
+
+struct View {
+  int slot = -1;
+  long long off = 0;
+  int dt = C64;
+  int nd = 0;
+  int d[4] = {1, 1, 1, 1};
+  long long s[4] = {0, 0, 0, 0};
+
+  View swap(int a, int b) const {
+    View r = *this;
+    std::swap(r.d[a], r.d[b]);
+    std::swap(r.s[a], r.s[b]);
+    return r;
+  }
+  long long numel() const {
+    long long x = 1;
+    for (int i = 0; i < nd; ++i) x *= d[i];
+    return x;
+  }
+};
+
+struct Term {
+  double cr = 1.0, ci = 0.0;
+  View A;
+  View B;  // slot -1: absent
+};
+
+enum OpKind { OP_GEMM = 0, OP_ADD = 1, OP_TRACE = 2 };
+
+enum GemmBackend { GB_FP64 = 0, GB_TC = 1 };
+
+struct Op {
+  OpKind kind;
+  std::string tag;
+  // GEMM
+  int sa = -1, sb = -1, sc = -1;
+  long long oa = 0, ob = 0, oc = 0;
+  int dta = C64, dtb = C64, dtc = C64;
+  GemmArgs g{};
+  int backend = GB_FP64;
+  long long flops = 0;     // real flops of this contraction
+  long long bytes = 0;     // compulsory bytes read + written
+  // ADD
+  AddArgs a{};
+  int add_slots[kMaxAddTerms][2];
+  long long add_off[kMaxAddTerms][2];
+  int add_sc = -1;
+  long long add_oc = 0;
+  // TRACE: res[k] = sum over 4 density blocks of mu_k * rho (see kernels)
+  int tr_slots[4];
+  int tr_n_mu = 0;
+  // dependency analysis
+  std::vector<int> reads;
+  int write = -1;
+  bool varying = true;
+};
+
+struct SlotInfo {
+  std::string name;
+  int dt;
+  long long numel;
+  bool fixed;
+  std::vector<double> init;  // uploaded at allocation (constant slots)
+};
+
+struct Dims {  // system sizes
+  int o, v, n;
+};
+
+class Program {
+ public:
+  Program(Dims dims, std::string name);
+
+  Dims dims;
+  std::string name;
+  std::vector<SlotInfo> slots;
+  std::vector<Op> ops;
+  long long flops_total = 0;
+
+  // views of fixed slots
+  View G(const char* blk) const;             // TEI block, e.g. "oovv"
+  View Fb(const char* blk) const;            // dressed Fock block "ov"
+  View amp(int slot) const;                  // T1/T2/L1/L2 view
+  View out(int nd) const;                    // output view (o,v) or (o,o,v,v)
+
+  // workspace tensor of the given shape ('o'/'v' letters), contiguous
+  View ws(const std::string& nm, const char* shape, int dt = C64);
+  View ws_dims(const std::string& nm, int nd, const int* d, int dt = C64);
+  // constant real vector of ones of length `len` (column sums via GEMM)
+  View ones(const std::string& nm, int len);
+
+  // C (+)= alpha * einsum(spec, A, B)
+  void ein(const char* spec, double ar, double ai, const View& A, const View& B,
+           const View& C, bool acc);
+  void ein(const char* spec, double alpha, const View& A, const View& B, const View& C,
+           bool acc) {
+    ein(spec, alpha, 0.0, A, B, C, acc);
+  }
+  // C (+)= sum_t coef_t * A_t (* B_t); all term views have C's dims
+  void add(const View& C, bool acc, const std::vector<Term>& terms);
+  void copy(const View& C, const View& A, double c = 1.0) { add(C, false, {Term{c, 0.0, A, View{}}}); }
+  void zero(const View& C) { add(C, false, {}); }
+  void trace(int n_mu, const View& Dij, const View& L1, const View& Dai, const View& Dab);
+
+  // antisymmetrisers applied while accumulating X into C
+  void acc_pij(const View& C, const View& X, double c = 1.0);     // C += c(X - X^(ij))
+  void acc_pab(const View& C, const View& X, double c = 1.0);     // C += c(X - X^(ab))
+  void acc_pijab(const View& C, const View& X, double c = 1.0);   // C += c P(ij)P(ab) X
+
+  // broadcast view: x with index string `from` seen with the indices `to`
+  static View bc(const View& x, const char* from, const char* to);
+
+  // marks ops that (transitively) read one of the varying slots
+  void analyse(const std::vector<int>& varying_slots);
+
+  // device allocation of workspace slots (returns bytes allocated)
+  long long allocate(std::vector<void*>& bases, std::vector<void*>& owned);
+
+  enum Phase { ALL = 0, PROLOGUE = 1, STAGE = 2 };
+  // `timed`, when given, receives (op, start event, stop event) per launch;
+  // the caller synchronises and destroys the events.
+  struct Timed {
+    const Op* op;
+    cudaEvent_t a, b;
+  };
+  cudaError_t run(const std::vector<void*>& bases, cudaStream_t st, Phase ph,
+                  std::vector<Timed>* timed = nullptr) const;
+
+  // mixed precision: which GEMMs go to the tensor-core backend
+  void select_backend(int prec_mode, long long min_flops);
+};
+
+// kernel launchers (kernels.cu)
+cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cudaStream_t st);
+cudaError_t launch_add(const AddArgs& a, cudaStream_t st);
+cudaError_t launch_trace(int n, int o, int n_mu, const double* mu, const void* dij,
+                         const void* l1, const void* dai, const void* dab, void* res,
+                         cudaStream_t st);
+void count_launch(long long k = 1);
+long long launch_count();
+
+// error reporting (capi.cpp)
+void set_error(const std::string& msg);
+
+}  // namespace tdcc

@@ -1,0 +1,333 @@
+// FP64 kernels of the plain form: strided tensor contraction (GEMM over
+// flattened mode groups), elementwise accumulate with antisymmetrisers, and
+// the dipole trace.  All complex data is interleaved (double2).
+#include <atomic>
+#include <cstdio>
+#include <type_traits>
+
+#include "engine.h"
+
+namespace tdcc {
+
+static std::atomic<long long> g_launches{0};
+void count_launch(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(); }
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+template <bool CPLX>
+struct Elem;
+template <>
+struct Elem<true> {
+  using T = double2;
+};
+template <>
+struct Elem<false> {
+  using T = double;
+};
+
+__device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
+
+__device__ __forceinline__ double2 as2(double x) { return make_double2(x, 0.0); }
+__device__ __forceinline__ double2 as2(double2 x) { return x; }
+
+// acc += a * b for the four real/complex combinations
+__device__ __forceinline__ void mac(double2& c, double a, double b) { c.x = fma(a, b, c.x); }
+__device__ __forceinline__ void mac(double2& c, double a, double2 b) {
+  c.x = fma(a, b.x, c.x);
+  c.y = fma(a, b.y, c.y);
+}
+__device__ __forceinline__ void mac(double2& c, double2 a, double b) {
+  c.x = fma(a.x, b, c.x);
+  c.y = fma(a.y, b, c.y);
+}
+__device__ __forceinline__ void mac(double2& c, double2 a, double2 b) {
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+}
+
+__device__ __forceinline__ void decomp(const ModeGroup& g, int l, long long& o0, long long& o1) {
+  o0 = 0;
+  o1 = 0;
+#pragma unroll
+  for (int q = kMaxModes - 1; q >= 0; --q) {
+    if (q < g.n) {
+      const int d = g.dim[q];
+      const int r = l % d;
+      l /= d;
+      o0 += (long long)r * g.s0[q];
+      o1 += (long long)r * g.s1[q];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 contraction: C[m,n] (+)= alpha * sum_k A[m,k] B[k,n]
+// 64x64 output tile, K step 16, 256 threads, 4x4 outputs per thread (strided
+// by 16 so shared-memory reads are conflict free).  On GB300 the FP64 pipe
+// (~1.2 TFLOP/s) is the bound, so the tile favours occupancy over reuse.
+// ---------------------------------------------------------------------------
+constexpr int GBM = 64, GBN = 64, GBK = 16;
+
+template <bool AC, bool BC, bool CC>
+__global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
+  using TA = typename Elem<AC>::T;
+  using TB = typename Elem<BC>::T;
+  __shared__ TA As[GBK][GBM];
+  __shared__ TB Bs[GBK][GBN];
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+  const int kbeg = blockIdx.z * g.kchunk;
+  const int kend = min(g.K, kbeg + g.kchunk);
+
+  const TA* A = static_cast<const TA*>(g.A);
+  const TB* B = static_cast<const TB*>(g.B);
+
+  // this thread's load row (A) / column (B) and its base offsets
+  const int lr = tid & 63;
+  const int lk = tid >> 6;  // 0..3
+  const int am = m0 + lr, bn = n0 + lr;
+  long long aoff = 0, boff = 0, dummy;
+  if (am < g.M) decomp(g.gm, am, aoff, dummy);
+  if (bn < g.N) decomp(g.gn, bn, boff, dummy);
+
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = cz();
+
+  for (int k0 = kbeg; k0 < kend; k0 += GBK) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int kk = lk + 4 * r;
+      const int k = k0 + kk;
+      TA av{};
+      TB bv{};
+      if (k < kend) {
+        long long ka, kb;
+        decomp(g.gk, k, ka, kb);
+        if (am < g.M) av = A[aoff + ka];
+        if (bn < g.N) bv = B[boff + kb];
+      }
+      As[kk][lr] = av;
+      Bs[kk][lr] = bv;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < GBK; ++kk) {
+      TA a[4];
+      TB b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mac(acc[i][j], a[i], b[j]);
+    }
+    __syncthreads();
+  }
+
+  long long coffm[4], coffn[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + ty + 16 * i;
+    coffm[i] = 0;
+    if (m < g.M) decomp(g.gm, m, dummy, coffm[i]);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int n = n0 + tx + 16 * j;
+    coffn[j] = 0;
+    if (n < g.N) decomp(g.gn, n, dummy, coffn[j]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + ty + 16 * i;
+    if (m >= g.M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int n = n0 + tx + 16 * j;
+      if (n >= g.N) continue;
+      const double2 s = acc[i][j];
+      const long long off = coffm[i] + coffn[j];
+      if constexpr (CC) {
+        double2* C = static_cast<double2*>(g.C);
+        const double2 v = make_double2(g.ar * s.x - g.ai * s.y, g.ar * s.y + g.ai * s.x);
+        if (g.atomic) {
+          atomicAdd(&C[off].x, v.x);
+          atomicAdd(&C[off].y, v.y);
+        } else if (g.acc) {
+          double2 c = C[off];
+          c.x += v.x;
+          c.y += v.y;
+          C[off] = c;
+        } else {
+          C[off] = v;
+        }
+      } else {
+        double* C = static_cast<double*>(g.C);
+        const double v = g.ar * s.x;
+        if (g.atomic)
+          atomicAdd(&C[off], v);
+        else if (g.acc)
+          C[off] += v;
+        else
+          C[off] = v;
+      }
+    }
+  }
+}
+
+cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cudaStream_t st) {
+  GemmArgs g = op.g;
+  g.A = A;
+  g.B = B;
+  g.C = C;
+  const int gx = (g.N + GBN - 1) / GBN, gy = (g.M + GBM - 1) / GBM;
+  const int gz = (g.K + g.kchunk - 1) / g.kchunk;
+  dim3 grid(gx, gy, gz);
+  if (gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
+  const bool ac = op.dta == C64, bc = op.dtb == C64, cc = op.dtc == C64;
+  if (ac && bc)
+    gemm_f64_kernel<true, true, true><<<grid, 256, 0, st>>>(g);
+  else if (ac && !bc)
+    gemm_f64_kernel<true, false, true><<<grid, 256, 0, st>>>(g);
+  else if (!ac && bc)
+    gemm_f64_kernel<false, true, true><<<grid, 256, 0, st>>>(g);
+  else if (cc)
+    gemm_f64_kernel<false, false, true><<<grid, 256, 0, st>>>(g);
+  else
+    gemm_f64_kernel<false, false, false><<<grid, 256, 0, st>>>(g);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// elementwise: C[idx] (+)= sum_t coef_t * A_t[idx] (* B_t[idx])
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 ld(const void* p, long long off, int cplx) {
+  if (cplx) return static_cast<const double2*>(p)[off];
+  return make_double2(static_cast<const double*>(p)[off], 0.0);
+}
+
+__global__ void __launch_bounds__(256) add_kernel(const AddArgs a) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < a.total; idx += stride) {
+    long long l = idx;
+    const int i3 = (int)(l % a.d[3]);
+    l /= a.d[3];
+    const int i2 = (int)(l % a.d[2]);
+    l /= a.d[2];
+    const int i1 = (int)(l % a.d[1]);
+    const int i0 = (int)(l / a.d[1]);
+    double2 s = cz();
+    for (int t = 0; t < a.nt; ++t) {
+      const AddTerm& T = a.t[t];
+      const long long oa = i0 * T.sA[0] + i1 * T.sA[1] + i2 * T.sA[2] + i3 * T.sA[3];
+      double2 x = ld(T.A, oa, T.ac);
+      if (T.B) {
+        const long long ob = i0 * T.sB[0] + i1 * T.sB[1] + i2 * T.sB[2] + i3 * T.sB[3];
+        const double2 y = ld(T.B, ob, T.bc);
+        x = make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+      }
+      s.x += T.cr * x.x - T.ci * x.y;
+      s.y += T.cr * x.y + T.ci * x.x;
+    }
+    const long long oc = i0 * a.sC[0] + i1 * a.sC[1] + i2 * a.sC[2] + i3 * a.sC[3];
+    if (a.cc) {
+      double2* C = static_cast<double2*>(a.C);
+      if (a.acc) {
+        double2 c = C[oc];
+        c.x += s.x;
+        c.y += s.y;
+        C[oc] = c;
+      } else {
+        C[oc] = s;
+      }
+    } else {
+      double* C = static_cast<double*>(a.C);
+      C[oc] = a.acc ? C[oc] + s.x : s.x;
+    }
+  }
+}
+
+cudaError_t launch_add(const AddArgs& a, cudaStream_t st) {
+  if (a.total <= 0) return cudaSuccess;
+  long long blocks = (a.total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  add_kernel<<<(unsigned)blocks, 256, 0, st>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// dipole trace: res[k] = sum_ij mu_k[i,j] rho[i,j], rho = [[Dij, l1],[Dai, Dab]]
+// One CTA per dipole component; warp-shuffle + shared-memory reduction, so
+// the sum order is fixed (deterministic).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) trace_kernel(int n, int o, const double* mu,
+                                                     const double2* dij, const double2* l1,
+                                                     const double2* dai, const double2* dab,
+                                                     double2* res) {
+  const int k = blockIdx.x;
+  const int v = n - o;
+  const double* M = mu + (long long)k * n * n;
+  double sr = 0.0, si = 0.0;
+  const long long nn = (long long)n * n;
+  for (long long e = threadIdx.x; e < nn; e += blockDim.x) {
+    const int p = (int)(e / n), q = (int)(e % n);
+    double2 r;
+    if (p < o && q < o)
+      r = dij[p * o + q];
+    else if (p < o)
+      r = l1[p * v + (q - o)];
+    else if (q < o)
+      r = dai[(p - o) * o + q];
+    else
+      r = dab[(long long)(p - o) * v + (q - o)];
+    const double m = M[e];
+    sr = fma(m, r.x, sr);
+    si = fma(m, r.y, si);
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, d);
+    si += __shfl_down_sync(0xffffffffu, si, d);
+  }
+  __shared__ double wr[32], wi[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    wr[w] = sr;
+    wi[w] = si;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    sr = lane < nw ? wr[lane] : 0.0;
+    si = lane < nw ? wi[lane] : 0.0;
+    for (int d = 16; d > 0; d >>= 1) {
+      sr += __shfl_down_sync(0xffffffffu, sr, d);
+      si += __shfl_down_sync(0xffffffffu, si, d);
+    }
+    if (lane == 0) res[k] = make_double2(sr, si);
+  }
+}
+
+cudaError_t launch_trace(int n, int o, int n_mu, const double* mu, const void* dij, const void* l1,
+                         const void* dai, const void* dab, void* res, cudaStream_t st) {
+  trace_kernel<<<n_mu, 1024, 0, st>>>(n, o, mu, static_cast<const double2*>(dij),
+                                      static_cast<const double2*>(l1),
+                                      static_cast<const double2*>(dai),
+                                      static_cast<const double2*>(dab), static_cast<double2*>(res));
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace tdcc

@@ -1,0 +1,453 @@
+// Programs: ordered op lists over symbolic buffer slots.  The einsum planner
+// turns "mnef,mnaf->ae" on strided views into a GEMM over flattened mode
+// groups (no permute copies); `analyse` splits a program into a prologue
+// (ops independent of the RK4 block's varying inputs, run once per step)
+// and the per-stage body.
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+
+#include "engine.h"
+
+namespace tdcc {
+
+Program::Program(Dims d, std::string nm) : dims(d), name(std::move(nm)) {
+  const long long n = d.n, o = d.o, v = d.v;
+  slots.resize(kNumFixedSlots);
+  slots[S_TEI] = {"tei", R64, n * n * n * n, true};
+  slots[S_F] = {"F", C64, n * n, true};
+  slots[S_T1] = {"t1", C64, o * v, true};
+  slots[S_T2] = {"t2", C64, o * o * v * v, true};
+  slots[S_L1] = {"l1", C64, o * v, true};
+  slots[S_L2] = {"l2", C64, o * o * v * v, true};
+  slots[S_OUT] = {"out", C64, o * o * v * v, true};
+  slots[S_MU] = {"mu", R64, 3 * n * n, true};
+  slots[S_RES] = {"res", C64, 3, true};
+}
+
+static int extent(const Dims& d, char c) {
+  if (c == 'o') return d.o;
+  if (c == 'v') return d.v;
+  throw std::runtime_error(std::string("bad block letter ") + c);
+}
+
+View Program::G(const char* blk) const {
+  View x;
+  x.slot = S_TEI;
+  x.dt = R64;
+  x.nd = 4;
+  const long long n = dims.n;
+  const long long st[4] = {n * n * n, n * n, n, 1};
+  x.off = 0;
+  for (int i = 0; i < 4; ++i) {
+    x.d[i] = extent(dims, blk[i]);
+    x.s[i] = st[i];
+    if (blk[i] == 'v') x.off += dims.o * st[i];
+  }
+  return x;
+}
+
+View Program::Fb(const char* blk) const {
+  View x;
+  x.slot = S_F;
+  x.dt = C64;
+  x.nd = 2;
+  const long long n = dims.n;
+  x.d[0] = extent(dims, blk[0]);
+  x.d[1] = extent(dims, blk[1]);
+  x.s[0] = n;
+  x.s[1] = 1;
+  x.off = (blk[0] == 'v' ? dims.o * n : 0) + (blk[1] == 'v' ? dims.o : 0);
+  return x;
+}
+
+View Program::amp(int slot) const {
+  View x;
+  x.slot = slot;
+  x.dt = C64;
+  const int o = dims.o, v = dims.v;
+  if (slot == S_T1 || slot == S_L1) {
+    x.nd = 2;
+    x.d[0] = o;
+    x.d[1] = v;
+    x.s[0] = v;
+    x.s[1] = 1;
+  } else {
+    x.nd = 4;
+    x.d[0] = o;
+    x.d[1] = o;
+    x.d[2] = v;
+    x.d[3] = v;
+    x.s[3] = 1;
+    x.s[2] = v;
+    x.s[1] = (long long)v * v;
+    x.s[0] = (long long)o * v * v;
+  }
+  return x;
+}
+
+View Program::out(int nd) const {
+  View x = amp(nd == 2 ? S_T1 : S_T2);
+  x.slot = S_OUT;
+  return x;
+}
+
+View Program::ws_dims(const std::string& nm, int nd, const int* d, int dt) {
+  View x;
+  x.slot = (int)slots.size();
+  x.dt = dt;
+  x.nd = nd;
+  long long st = 1;
+  for (int i = nd - 1; i >= 0; --i) {
+    x.d[i] = d[i];
+    x.s[i] = st;
+    st *= d[i];
+  }
+  slots.push_back({nm, dt, st, false});
+  return x;
+}
+
+View Program::ones(const std::string& nm, int len) {
+  int d[1] = {len};
+  View x = ws_dims(nm, 1, d, R64);
+  slots[x.slot].init.assign(len, 1.0);
+  return x;
+}
+
+View Program::ws(const std::string& nm, const char* shape, int dt) {
+  int d[4];
+  const int nd = (int)strlen(shape);
+  for (int i = 0; i < nd; ++i) d[i] = extent(dims, shape[i]);
+  return ws_dims(nm, nd, d, dt);
+}
+
+View Program::bc(const View& x, const char* from, const char* to) {
+  View r;
+  r.slot = x.slot;
+  r.off = x.off;
+  r.dt = x.dt;
+  r.nd = (int)strlen(to);
+  for (int i = 0; i < r.nd; ++i) {
+    const char* p = strchr(from, to[i]);
+    if (p) {
+      const int k = (int)(p - from);
+      r.d[i] = x.d[k];
+      r.s[i] = x.s[k];
+    } else {
+      r.d[i] = 1;  // caller fixes dims to match the target
+      r.s[i] = 0;
+    }
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// einsum -> GEMM over mode groups
+// ---------------------------------------------------------------------------
+void Program::ein(const char* spec, double ar, double ai, const View& A, const View& B,
+                  const View& C, bool acc) {
+  std::string s(spec);
+  const size_t comma = s.find(','), arrow = s.find("->");
+  if (comma == std::string::npos || arrow == std::string::npos)
+    throw std::runtime_error("einsum spec: " + s);
+  const std::string ia = s.substr(0, comma), ib = s.substr(comma + 1, arrow - comma - 1),
+                    ic = s.substr(arrow + 2);
+  if ((int)ia.size() != A.nd || (int)ib.size() != B.nd || (int)ic.size() != C.nd)
+    throw std::runtime_error("einsum rank mismatch: " + s);
+  auto dim_of = [&](char c) -> int {
+    size_t p;
+    if ((p = ia.find(c)) != std::string::npos) return A.d[p];
+    if ((p = ib.find(c)) != std::string::npos) return B.d[p];
+    return C.d[ic.find(c)];
+  };
+  // consistency of extents
+  for (size_t i = 0; i < ia.size(); ++i)
+    if (dim_of(ia[i]) != A.d[i]) throw std::runtime_error("einsum extent mismatch: " + s);
+  for (size_t i = 0; i < ib.size(); ++i)
+    if (dim_of(ib[i]) != B.d[i]) throw std::runtime_error("einsum extent mismatch: " + s);
+  for (size_t i = 0; i < ic.size(); ++i)
+    if (dim_of(ic[i]) != C.d[i]) throw std::runtime_error("einsum extent mismatch: " + s);
+
+  Op op;
+  op.kind = OP_GEMM;
+  op.tag = name + ":" + s;
+  GemmArgs& g = op.g;
+  memset(&g, 0, sizeof(g));
+  auto push = [&](ModeGroup& grp, int dim, long long s0, long long s1) {
+    if (grp.n >= kMaxModes) throw std::runtime_error("einsum: too many modes in a group: " + s);
+    grp.dim[grp.n] = dim;
+    grp.s0[grp.n] = s0;
+    grp.s1[grp.n] = s1;
+    grp.n++;
+  };
+  for (size_t i = 0; i < ic.size(); ++i) {
+    const char c = ic[i];
+    const size_t pa = ia.find(c), pb = ib.find(c);
+    if (pa != std::string::npos && pb != std::string::npos)
+      throw std::runtime_error("einsum: batch index unsupported: " + s);
+    if (pa != std::string::npos)
+      push(g.gm, C.d[i], A.s[pa], C.s[i]);
+    else if (pb != std::string::npos)
+      push(g.gn, C.d[i], B.s[pb], C.s[i]);
+    else
+      throw std::runtime_error("einsum: broadcast output index unsupported: " + s);
+  }
+  for (size_t i = 0; i < ia.size(); ++i) {
+    const char c = ia[i];
+    if (ic.find(c) != std::string::npos) continue;
+    if (ia.find(c) != i) throw std::runtime_error("einsum: repeated index: " + s);
+    const size_t pb = ib.find(c);
+    push(g.gk, A.d[i], A.s[i], pb != std::string::npos ? B.s[pb] : 0);
+  }
+  for (size_t i = 0; i < ib.size(); ++i) {
+    const char c = ib[i];
+    if (ic.find(c) != std::string::npos || ia.find(c) != std::string::npos) continue;
+    push(g.gk, B.d[i], 0, B.s[i]);
+  }
+  auto prod = [](const ModeGroup& grp) {
+    long long p = 1;
+    for (int i = 0; i < grp.n; ++i) p *= grp.dim[i];
+    return p;
+  };
+  const long long M = prod(g.gm), N = prod(g.gn), K = prod(g.gk);
+  if (M > (1LL << 31) - 1 || N > (1LL << 31) - 1 || K > (1LL << 31) - 1)
+    throw std::runtime_error("einsum: dimension too large: " + s);
+  g.M = (int)M;
+  g.N = (int)N;
+  g.K = (int)K;
+  g.ar = ar;
+  g.ai = ai;
+  g.acc = acc ? 1 : 0;
+  // split-K so that small output tiles still fill the 152 SMs
+  const long long tiles = ((M + 63) / 64) * ((N + 63) / 64);
+  long long splits = 1;
+  if (tiles < 2 * 152 && K >= 64) {
+    splits = (2 * 152 + tiles - 1) / tiles;
+    splits = std::min<long long>(splits, K / 32);
+    splits = std::max<long long>(splits, 1);
+  }
+  long long kchunk = (K + splits - 1) / splits;
+  kchunk = ((kchunk + 15) / 16) * 16;
+  g.kchunk = (int)std::max<long long>(kchunk, 16);
+  splits = (K + g.kchunk - 1) / g.kchunk;
+  g.atomic = splits > 1 ? 1 : 0;
+  op.sa = A.slot;
+  op.sb = B.slot;
+  op.sc = C.slot;
+  op.oa = A.off;
+  op.ob = B.off;
+  op.oc = C.off;
+  op.dta = A.dt;
+  op.dtb = B.dt;
+  op.dtc = C.dt;
+  if (C.dt == R64 && (A.dt == C64 || B.dt == C64))
+    throw std::runtime_error("einsum: complex product into real output: " + s);
+  const int mult = (A.dt == C64 && B.dt == C64) ? 8 : (A.dt == C64 || B.dt == C64) ? 4 : 2;
+  op.flops = mult * M * N * K;
+  auto esz = [](int dt) { return dt == C64 ? 16LL : 8LL; };
+  op.bytes = M * K * esz(A.dt) + K * N * esz(B.dt) + M * N * esz(C.dt) * (acc ? 2 : 1);
+  flops_total += op.flops;
+  op.reads = {A.slot, B.slot};
+  if (acc) op.reads.push_back(C.slot);
+  op.write = C.slot;
+  // split-K accumulates with atomics: zero the target first when overwriting
+  if (g.atomic && !acc) {
+    zero(C);
+    op.reads.push_back(C.slot);
+  }
+  ops.push_back(op);
+}
+
+void Program::add(const View& C, bool acc, const std::vector<Term>& terms) {
+  if ((int)terms.size() > kMaxAddTerms) throw std::runtime_error("add: too many terms");
+  Op op;
+  op.kind = OP_ADD;
+  op.tag = name + ":add";
+  AddArgs& a = op.a;
+  memset(&a, 0, sizeof(a));
+  for (int i = 0; i < 4; ++i) {
+    a.d[i] = i < C.nd ? C.d[i] : 1;
+    a.sC[i] = i < C.nd ? C.s[i] : 0;
+  }
+  // right-align so the last index is the fastest (C.nd may be < 4)
+  if (C.nd < 4) {
+    const int sh = 4 - C.nd;
+    for (int i = 3; i >= 0; --i) {
+      a.d[i] = i - sh >= 0 ? C.d[i - sh] : 1;
+      a.sC[i] = i - sh >= 0 ? C.s[i - sh] : 0;
+    }
+  }
+  a.total = C.numel();
+  a.cc = C.dt == C64;
+  a.acc = acc ? 1 : 0;
+  a.nt = (int)terms.size();
+  op.add_sc = C.slot;
+  op.add_oc = C.off;
+  op.write = C.slot;
+  if (acc) op.reads.push_back(C.slot);
+  const int sh = 4 - C.nd;
+  for (int t = 0; t < a.nt; ++t) {
+    const Term& T = terms[t];
+    if (T.A.nd != C.nd) throw std::runtime_error("add: term rank mismatch in " + name);
+    for (int i = 0; i < C.nd; ++i)
+      if (T.A.d[i] != C.d[i] && T.A.s[i] != 0) throw std::runtime_error("add: term dims mismatch in " + name);
+    AddTerm& at = a.t[t];
+    at.cr = T.cr;
+    at.ci = T.ci;
+    at.ac = T.A.dt == C64;
+    for (int i = 0; i < 4; ++i) at.sA[i] = i - sh >= 0 ? T.A.s[i - sh] : 0;
+    op.add_slots[t][0] = T.A.slot;
+    op.add_off[t][0] = T.A.off;
+    op.reads.push_back(T.A.slot);
+    if (T.B.slot >= 0) {
+      if (T.B.nd != C.nd) throw std::runtime_error("add: factor rank mismatch in " + name);
+      at.bc = T.B.dt == C64;
+      for (int i = 0; i < 4; ++i) at.sB[i] = i - sh >= 0 ? T.B.s[i - sh] : 0;
+      op.add_slots[t][1] = T.B.slot;
+      op.add_off[t][1] = T.B.off;
+      op.reads.push_back(T.B.slot);
+    } else {
+      op.add_slots[t][1] = -1;
+      op.add_off[t][1] = 0;
+    }
+    if (C.dt == R64 && (at.ac || at.bc || T.ci != 0.0))
+      throw std::runtime_error("add: complex term into real output in " + name);
+  }
+  {
+    const long long e = a.cc ? 16 : 8;
+    long long nread = a.nt + (acc ? 1 : 0);
+    for (int t = 0; t < a.nt; ++t)
+      if (op.add_slots[t][1] >= 0) ++nread;
+    op.bytes = a.total * e * (nread + 1);
+  }
+  ops.push_back(op);
+}
+
+void Program::trace(int n_mu, const View& Dij, const View& L1, const View& Dai, const View& Dab) {
+  Op op;
+  op.kind = OP_TRACE;
+  op.tag = name + ":trace";
+  op.tr_slots[0] = Dij.slot;
+  op.tr_slots[1] = L1.slot;
+  op.tr_slots[2] = Dai.slot;
+  op.tr_slots[3] = Dab.slot;
+  op.tr_n_mu = n_mu;
+  op.reads = {Dij.slot, L1.slot, Dai.slot, Dab.slot, S_MU};
+  op.write = S_RES;
+  ops.push_back(op);
+}
+
+void Program::acc_pij(const View& C, const View& X, double c) {
+  add(C, true, {Term{c, 0, X, View{}}, Term{-c, 0, X.swap(0, 1), View{}}});
+}
+void Program::acc_pab(const View& C, const View& X, double c) {
+  add(C, true, {Term{c, 0, X, View{}}, Term{-c, 0, X.swap(2, 3), View{}}});
+}
+void Program::acc_pijab(const View& C, const View& X, double c) {
+  add(C, true,
+      {Term{c, 0, X, View{}}, Term{-c, 0, X.swap(2, 3), View{}}, Term{-c, 0, X.swap(0, 1), View{}},
+       Term{c, 0, X.swap(0, 1).swap(2, 3), View{}}});
+}
+
+// ---------------------------------------------------------------------------
+// dependency analysis
+// ---------------------------------------------------------------------------
+void Program::analyse(const std::vector<int>& varying_slots) {
+  std::vector<char> vs(slots.size(), 0);
+  for (int s : varying_slots) vs[s] = 1;
+  vs[S_OUT] = 1;
+  for (auto& op : ops) op.varying = false;
+  bool changed = true;
+  while (changed) {
+    changed = false;
+    for (auto& op : ops) {
+      bool v = op.varying;
+      for (int r : op.reads)
+        if (r >= 0 && vs[r]) v = true;
+      if (op.write >= 0 && vs[op.write]) v = true;
+      if (v && !op.varying) {
+        op.varying = true;
+        changed = true;
+      }
+      if (v && op.write >= 0 && !vs[op.write]) {
+        vs[op.write] = 1;
+        changed = true;
+      }
+    }
+  }
+}
+
+long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned) {
+  long long bytes = 0;
+  if (bases.size() < slots.size()) bases.resize(slots.size(), nullptr);
+  for (size_t i = kNumFixedSlots; i < slots.size(); ++i) {
+    const size_t b = (size_t)slots[i].numel * (slots[i].dt == C64 ? 16 : 8);
+    void* p = nullptr;
+    if (cudaMalloc(&p, b) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::runtime_error("cudaMalloc failed for workspace " + slots[i].name + " in " + name);
+    }
+    owned.push_back(p);
+    bases[i] = p;
+    if (!slots[i].init.empty() &&
+        cudaMemcpy(p, slots[i].init.data(), slots[i].init.size() * sizeof(double),
+                   cudaMemcpyHostToDevice) != cudaSuccess)
+      throw std::runtime_error("upload of constant slot " + slots[i].name + " failed");
+    bytes += (long long)b;
+  }
+  return bytes;
+}
+
+static inline const void* at(const std::vector<void*>& b, int slot, long long off, int dt) {
+  const char* p = static_cast<const char*>(b[slot]);
+  return p + off * (dt == C64 ? 16 : 8);
+}
+
+cudaError_t Program::run(const std::vector<void*>& bases, cudaStream_t st, Phase ph,
+                         std::vector<Timed>* timed) const {
+  for (const auto& op : ops) {
+    if (ph == PROLOGUE && op.varying) continue;
+    if (ph == STAGE && !op.varying) continue;
+    cudaError_t e = cudaSuccess;
+    Timed tm{&op, nullptr, nullptr};
+    if (timed) {
+      cudaEventCreate(&tm.a);
+      cudaEventCreate(&tm.b);
+      cudaEventRecord(tm.a, st);
+    }
+    if (op.kind == OP_GEMM) {
+      e = launch_gemm(op, at(bases, op.sa, op.oa, op.dta), at(bases, op.sb, op.ob, op.dtb),
+                      const_cast<void*>(at(bases, op.sc, op.oc, op.dtc)), st);
+    } else if (op.kind == OP_ADD) {
+      AddArgs a = op.a;
+      a.C = const_cast<void*>(at(bases, op.add_sc, op.add_oc, a.cc ? C64 : R64));
+      for (int t = 0; t < a.nt; ++t) {
+        a.t[t].A = at(bases, op.add_slots[t][0], op.add_off[t][0], a.t[t].ac ? C64 : R64);
+        a.t[t].B = op.add_slots[t][1] >= 0
+                       ? at(bases, op.add_slots[t][1], op.add_off[t][1], a.t[t].bc ? C64 : R64)
+                       : nullptr;
+      }
+      e = launch_add(a, st);
+    } else if (op.kind == OP_TRACE) {
+      e = launch_trace(dims.n, dims.o, op.tr_n_mu, static_cast<const double*>(bases[S_MU]),
+                       bases[op.tr_slots[0]], bases[op.tr_slots[1]], bases[op.tr_slots[2]],
+                       bases[op.tr_slots[3]], bases[S_RES], st);
+    }
+    if (timed) {
+      cudaEventRecord(tm.b, st);
+      timed->push_back(tm);
+    }
+    if (e != cudaSuccess) {
+      set_error("kernel launch failed in " + op.tag + ": " + cudaGetErrorString(e));
+      return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+void Program::select_backend(int prec_mode, long long min_flops) {
+  for (auto& op : ops)
+    if (op.kind == OP_GEMM) op.backend = (prec_mode == 1 && op.flops >= min_flops) ? GB_TC : GB_FP64;
+}
+
+}  // namespace tdcc

@@ -1,0 +1,167 @@
+// HBM-bound kernels of the block-frozen RK4 propagator: field evaluation,
+// Fock dressing, the fused stage axpys and the rounded final update.
+// Reference: CCSD_Helper.py:1158-1240 (ft1/ft2/fL1/fL2, Runge_Kutta_solver).
+#include <cmath>
+
+#include "rk4.h"
+
+namespace tdcc {
+
+__device__ double2 field_value(const tdcc_field& f, double t) {
+  switch (f.kind) {
+    case TDCC_FIELD_SIN:
+      return make_double2(f.A * sin(f.w0 * t), 0.0);
+    case TDCC_FIELD_REFERENCE: {
+      // cmath.exp(1j*w0*2*np.pi*t): phase evaluated as ((w0*2)*pi)*t
+      const double th = ((f.w0 * 2.0) * 3.141592653589793) * t;
+      return make_double2(f.A * cos(th), f.A * sin(th));
+    }
+    case TDCC_FIELD_ENVELOPE: {
+      double env = 0.0;
+      for (int k = 0; k < f.n_env; ++k) {
+        const double d = (t - (f.env_t0 + k * f.env_dt)) / f.env_sigma;
+        env += f.env_c[k] * exp(-0.5 * d * d);
+      }
+      return make_double2(f.A * sin(f.w0 * t) * env, 0.0);
+    }
+    default:
+      return make_double2(0.0, 0.0);
+  }
+}
+
+// ctx->t += dt (the reference advances t before the stages), then the field
+// at t, t + dt/2, t + dt.
+__global__ void advance_field_kernel(StepCtx* ctx) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const double t = __dadd_rn(ctx->t, ctx->dt);
+    ctx->t = t;
+    const double h = ctx->dt / 2.0;
+    ctx->E[0] = field_value(ctx->field, t);
+    ctx->E[1] = field_value(ctx->field, __dadd_rn(t, h));
+    ctx->E[2] = field_value(ctx->field, __dadd_rn(t, ctx->dt));
+  }
+}
+
+// Fs[s] = fock - E[s] * mu_z  for the three stage times
+__global__ void dress_kernel(const StepCtx* ctx, const double* __restrict__ fock,
+                             const double* __restrict__ muz, double2* __restrict__ Fs, int nn) {
+  const int s = blockIdx.y;
+  const double2 E = ctx->E[s];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += gridDim.x * blockDim.x) {
+    const double m = muz[e];
+    Fs[(long long)s * nn + e] = make_double2(fock[e] - E.x * m, -(E.y * m));
+  }
+}
+
+// Stage s (1..4) after k_s is known:
+//   s=1: acc = k            ; yin = y0 + (dt/2) k
+//   s=2: acc = acc + 2k     ; yin = y0 + (dt/2) k
+//   s=3: acc = acc + 2k     ; yin = y0 + dt k
+//   s=4: acc = acc + k
+// Evaluation order and roundings follow numpy's for
+// dt/6.0*(k1 + 2.0*k2 + 2.0*k3 + k4) and t + dt/2.0*k (no FMA contraction).
+__global__ void rk4_stage_kernel(const double2* __restrict__ y0, const double2* __restrict__ k,
+                                 double2* __restrict__ acc, double2* __restrict__ yin, long long n,
+                                 int s, double h) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 kk = k[i];
+    double2 a;
+    if (s == 1) {
+      a = kk;
+    } else {
+      a = acc[i];
+      if (s == 4) {
+        a.x = __dadd_rn(a.x, kk.x);
+        a.y = __dadd_rn(a.y, kk.y);
+      } else {
+        a.x = __dadd_rn(a.x, __dmul_rn(2.0, kk.x));
+        a.y = __dadd_rn(a.y, __dmul_rn(2.0, kk.y));
+      }
+    }
+    acc[i] = a;
+    if (s < 4) {
+      const double2 y = y0[i];
+      yin[i] = make_double2(__dadd_rn(y.x, __dmul_rn(h, kk.x)), __dadd_rn(y.y, __dmul_rn(h, kk.y)));
+    }
+  }
+}
+
+__device__ __forceinline__ double round_dec(double x, double scale) {
+  // np.around(x, decimals): rint(x * 10**decimals) / 10**decimals
+  return __ddiv_rn(rint(__dmul_rn(x, scale)), scale);
+}
+
+// ynew = round(y0, precs) + sign_i * (dt/6) * acc, sign_i = -i (T) or +i (Lambda)
+__global__ void rk4_finish_kernel(const double2* __restrict__ y0, const double2* __restrict__ acc,
+                                  double2* __restrict__ ynew, long long n, double dt6, int sign,
+                                  double scale, int do_round) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 a = acc[i];
+    const double dx = __dmul_rn(dt6, a.x), dy = __dmul_rn(dt6, a.y);
+    // (-1j)*(dx + i dy) = dy - i dx ; (+1j)*(dx + i dy) = -dy + i dx
+    const double2 d = sign < 0 ? make_double2(dy, -dx) : make_double2(-dy, dx);
+    double2 y = y0[i];
+    if (do_round) {
+      y.x = round_dec(y.x, scale);
+      y.y = round_dec(y.y, scale);
+    }
+    ynew[i] = make_double2(__dadd_rn(y.x, d.x), __dadd_rn(y.y, d.y));
+  }
+}
+
+__global__ void record_mu_kernel(StepCtx* ctx, const double2* res, int n_mu, double2* traj,
+                                 double* times) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const long long s = ctx->step;
+    if (traj) traj[s] = res[n_mu - 1];
+    if (times) times[s] = ctx->t;
+    ctx->step = s + 1;
+  }
+}
+
+static unsigned grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+cudaError_t launch_advance_field(StepCtx* ctx, cudaStream_t st) {
+  advance_field_kernel<<<1, 32, 0, st>>>(ctx);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dress(const StepCtx* ctx, const double* fock, const double* muz, double2* Fs,
+                         int n, cudaStream_t st) {
+  const int nn = n * n;
+  dim3 grid((nn + 255) / 256 > 64 ? 64 : (nn + 255) / 256, 3);
+  dress_kernel<<<grid, 256, 0, st>>>(ctx, fock, muz, Fs, nn);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rk4_stage(const double2* y0, const double2* k, double2* acc, double2* yin,
+                             long long n, int s, double h, cudaStream_t st) {
+  rk4_stage_kernel<<<grid_for(n), 256, 0, st>>>(y0, k, acc, yin, n, s, h);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rk4_finish(const double2* y0, const double2* acc, double2* ynew, long long n,
+                              double dt6, int sign, double scale, int do_round, cudaStream_t st) {
+  rk4_finish_kernel<<<grid_for(n), 256, 0, st>>>(y0, acc, ynew, n, dt6, sign, scale, do_round);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_record_mu(StepCtx* ctx, const double2* res, int n_mu, double2* traj,
+                             double* times, cudaStream_t st) {
+  record_mu_kernel<<<1, 32, 0, st>>>(ctx, res, n_mu, traj, times);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace tdcc

@@ -1,0 +1,190 @@
+"""GPU engine: a tdcc_system on one CUDA device, driven through the C ABI.
+
+``CCEngine`` owns the device copies of the integrals and the native handle.
+Its methods carry the reference's names (``CCSD_Helper`` / ``CC2_Helper``)
+so code written against the reference reads the same:
+
+===========================  =================================================
+reference (file:line)        here
+===========================  =================================================
+T1eq_rhs  CCSD_Helper.py:177 ``T1eq_rhs(t1, t2, F)``
+T2eq_rhs  CCSD_Helper.py:268 ``T2eq_rhs(t1, t2, F)``
+lam_1eq_rhs  :555            ``lam_1eq_rhs(t1, t2, l1, l2, F)``
+lam2eq_rhs   :610            ``lam2eq_rhs(t1, t2, l1, l2, F)``
+T2eq_rhs_CC2 CC2_Helper.py:12 ``T2eq_rhs_CC2(t1, t2, F)``
+L1eq_rhs_CC2 CC2_Helper.py:50 ``L1eq_rhs_CC2(t1, t2, l1, l2, F)``
+L2eq_rhs_CC2 CC2_Helper.py:128 ``L2eq_rhs_CC2(t1, t2, l1, l2, F)``
+dipole_moment CCSD_Helper.py:1066 ``dipole_moment(t1, t2, l1, l2)``
+loop body CCSD_Helper.py:1206 ``rk4_step(method, state, t_prev, dt, field, precs)``
+===========================  =================================================
+
+Arrays may be numpy or torch; results are torch complex128 CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import TDCC_CC2, TDCC_CCSD, TDCC_L1, TDCC_L2, TDCC_T1, TDCC_T2, check
+
+
+def _dev():
+    if not torch.cuda.is_available():
+        raise _lib.TdccError("no CUDA device: the TD-CC engine runs on the GPU only")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def to_dev(x, dtype=torch.complex128):
+    dev = _dev()
+    if isinstance(x, torch.Tensor):
+        return x.to(device=dev, dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device=dev).contiguous()
+
+
+def _ptr(x):
+    return ctypes.c_void_p(x.data_ptr()) if x is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class CCEngine:
+    """One synthetic (or psi4-provided) system resident on the GPU."""
+
+    def __init__(self, tei, fock, mu, o: int):
+        self.lib = _lib.load()
+        self.tei = to_dev(tei, torch.float64)
+        self.fock = to_dev(fock, torch.float64)
+        mus = [m for m in mu] if isinstance(mu, (list, tuple)) else [mu]
+        self.mu = torch.stack([to_dev(m, torch.float64) for m in mus]).contiguous()
+        self.n = int(self.fock.shape[0])
+        self.o = int(o)
+        self.v = self.n - self.o
+        if tuple(self.tei.shape) != (self.n,) * 4:
+            raise ValueError("tei must be (n,n,n,n)")
+        h = ctypes.c_void_p()
+        check(self.lib.tdcc_system_create(self.o, self.v, _ptr(self.tei), _ptr(self.fock),
+                                          _ptr(self.mu), int(self.mu.shape[0]), ctypes.byref(h)),
+              "tdcc_system_create")
+        self.handle = h
+        self.precision = "fp64"
+
+    @classmethod
+    def from_system(cls, sysm):
+        return cls(sysm.tei(), sysm.fock, sysm.mu, sysm.o)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.tdcc_system_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- configuration ----
+    def set_precision(self, mode: str = "fp64", slices: int = 5):
+        m = {"fp64": _lib.TDCC_PREC_FP64, "mixed": _lib.TDCC_PREC_MIXED}[mode]
+        check(self.lib.tdcc_set_precision(self.handle, m, int(slices)), "tdcc_set_precision")
+        self.precision = mode
+
+    def workspace_bytes(self) -> int:
+        return int(self.lib.tdcc_workspace_bytes(self.handle))
+
+    # ---- residuals ----
+    def rhs(self, method: str, block: int, t1, t2, l1=None, l2=None, F=None):
+        m = _lib.METHODS[method]
+        t1 = to_dev(t1)
+        t2 = to_dev(t2)
+        l1 = to_dev(l1) if l1 is not None else None
+        l2 = to_dev(l2) if l2 is not None else None
+        F = to_dev(self.fock if F is None else F)
+        out = torch.empty_like(t1 if block in (TDCC_T1, TDCC_L1) else t2)
+        check(self.lib.tdcc_rhs(self.handle, m, block, _ptr(t1), _ptr(t2), _ptr(l1), _ptr(l2),
+                                _ptr(F), _ptr(out), _stream()), "tdcc_rhs")
+        return out
+
+    def T1eq_rhs(self, t1, t2, F):
+        return self.rhs("CCSD", TDCC_T1, t1, t2, F=F)
+
+    def T2eq_rhs(self, t1, t2, F):
+        return self.rhs("CCSD", TDCC_T2, t1, t2, F=F)
+
+    def lam_1eq_rhs(self, t1, t2, l1, l2, F):
+        return self.rhs("CCSD", TDCC_L1, t1, t2, l1, l2, F)
+
+    def lam2eq_rhs(self, t1, t2, l1, l2, F):
+        return self.rhs("CCSD", TDCC_L2, t1, t2, l1, l2, F)
+
+    def T2eq_rhs_CC2(self, t1, t2, F):
+        return self.rhs("CC2", TDCC_T2, t1, t2, F=F)
+
+    def L1eq_rhs_CC2(self, t1, t2, l1, l2, F):
+        return self.rhs("CC2", TDCC_L1, t1, t2, l1, l2, F)
+
+    def L2eq_rhs_CC2(self, t1, t2, l1, l2, F):
+        return self.rhs("CC2", TDCC_L2, t1, t2, l1, l2, F)
+
+    # ---- density / dipole ----
+    def dipole_moment(self, t1, t2, l1, l2, F=None):
+        t1, t2, l1, l2 = (to_dev(x) for x in (t1, t2, l1, l2))
+        out = torch.empty(int(self.mu.shape[0]), dtype=torch.complex128, device=t1.device)
+        check(self.lib.tdcc_dipole(self.handle, _ptr(t1), _ptr(t2), _ptr(l1), _ptr(l2), _ptr(out),
+                                   _stream()), "tdcc_dipole")
+        return out
+
+    # ---- propagation ----
+    def rk4_step(self, method: str, state, t_prev: float, dt: float, field, precs: int = 15,
+                 with_mu: bool = True):
+        """One reference loop-body step; returns (new_state, mu or None)."""
+        t1, t2, l1, l2 = (to_dev(x) for x in state)
+        outs = [torch.empty_like(x) for x in (t1, t2, l1, l2)]
+        mu = torch.empty(int(self.mu.shape[0]), dtype=torch.complex128, device=t1.device) if with_mu else None
+        check(self.lib.tdcc_rk4_step(self.handle, _lib.METHODS[method], _ptr(t1), _ptr(t2), _ptr(l1),
+                                     _ptr(l2), *(_ptr(x) for x in outs), float(t_prev), float(dt),
+                                     int(precs), ctypes.byref(field), _ptr(mu), _stream()),
+              "tdcc_rk4_step")
+        return tuple(outs), mu
+
+    def propagate(self, method: str, state, t0: float, dt: float, nsteps: int, field, precs: int = 15):
+        """nsteps device-resident steps (captured CUDA graph); returns
+        (final_state, mu_z trajectory as a complex128 CUDA tensor)."""
+        st = [to_dev(x).clone() for x in state]
+        traj = torch.empty(max(int(nsteps), 1), dtype=torch.complex128, device=st[0].device)
+        check(self.lib.tdcc_propagate(self.handle, _lib.METHODS[method], *(_ptr(x) for x in st),
+                                      float(t0), float(dt), int(nsteps), int(precs),
+                                      ctypes.byref(field), _ptr(traj), _stream()),
+              "tdcc_propagate")
+        return tuple(st), traj[: int(nsteps)]
+
+
+def profile_step(eng: "CCEngine", method: str, state, t_prev: float, dt: float, field, precs: int = 15):
+    """Per-kernel CUDA-event timings of one serial, eager RK4 step.  Returns a
+    list of dicts (tag, kind, block, stage, backend, flops, bytes, ms)."""
+    t1, t2, l1, l2 = (to_dev(x) for x in state)
+    cap = 8192
+    recs = (_lib.TdccOpRecord * cap)()
+    n = ctypes.c_int(0)
+    torch.cuda.synchronize()
+    check(eng.lib.tdcc_profile_step(eng.handle, _lib.METHODS[method], _ptr(t1), _ptr(t2), _ptr(l1),
+                                    _ptr(l2), float(t_prev), float(dt), int(precs), ctypes.byref(field),
+                                    recs, cap, ctypes.byref(n)), "tdcc_profile_step")
+    out = []
+    for k in range(min(n.value, cap)):
+        r = recs[k]
+        out.append(dict(tag=r.tag.decode(), kind=r.kind, block=r.block, stage=r.stage,
+                        backend=r.backend, flops=r.flops, bytes=r.bytes, ms=r.ms))
+    return out
+
+
+def launch_count() -> int:
+    return int(_lib.load().tdcc_launch_count())
+
+
+__all__ = ["CCEngine", "launch_count", "TDCC_CCSD", "TDCC_CC2", "TDCC_T1", "TDCC_T2", "TDCC_L1", "TDCC_L2"]

@@ -1,0 +1,94 @@
+"""numpy interpreter of libtdcc program op lists (from tdcc_program_json).
+
+Executes exactly the GEMM mode groups / strides / coefficients and the
+elementwise terms the GPU kernels receive, on flat host buffers, so the
+equation programs and their prologue/stage split can be checked on a CPU."""
+import numpy as np
+
+S_TEI, S_F, S_T1, S_T2, S_L1, S_L2, S_OUT, S_MU, S_RES = range(9)
+
+
+def _group(g):
+    n = g["n"]
+    if n == 0:
+        z = np.zeros(1, dtype=np.int64)
+        return z, z
+    idx = np.indices(g["dim"]).reshape(n, -1).astype(np.int64)
+    s0 = np.array(g["s0"], dtype=np.int64)[:, None]
+    s1 = np.array(g["s1"], dtype=np.int64)[:, None]
+    return (idx * s0).sum(0), (idx * s1).sum(0)
+
+
+class Emulator:
+    def __init__(self, prog, o, v, n_mu=3):
+        self.p = prog
+        self.o, self.v, self.n = o, v, o + v
+        self.n_mu = n_mu
+        self.bufs = {}
+        for i, s in enumerate(prog["slots"]):
+            if s["fixed"]:
+                continue
+            dt = np.complex128 if s["dt"] == 1 else np.float64
+            self.bufs[i] = np.ones(s["numel"], dtype=dt) if s["ones"] else np.zeros(s["numel"], dtype=dt)
+
+    def bind(self, slot, arr):
+        self.bufs[slot] = np.ascontiguousarray(arr).reshape(-1)
+
+    def run(self, phase="all"):
+        for op in self.p["ops"]:
+            if phase == "prologue" and op["varying"]:
+                continue
+            if phase == "stage" and not op["varying"]:
+                continue
+            getattr(self, "_" + op["kind"])(op)
+
+    def _gemm(self, op):
+        am, cm = _group(op["gm"])
+        bn, cn = _group(op["gn"])
+        ak, bk = _group(op["gk"])
+        A = self.bufs[op["sa"]]
+        B = self.bufs[op["sb"]]
+        C = self.bufs[op["sc"]]
+        Am = A[op["oa"] + am[:, None] + ak[None, :]]
+        Bm = B[op["ob"] + bk[:, None] + bn[None, :]]
+        val = complex(op["ar"], op["ai"]) * (Am @ Bm)
+        if C.dtype == np.float64:
+            val = val.real
+        idx = op["oc"] + cm[:, None] + cn[None, :]
+        if op["acc"] or op["atomic"]:
+            C[idx] += val
+        else:
+            C[idx] = val
+
+    def _add(self, op):
+        d = op["d"]
+        I = np.indices(d).reshape(4, -1).astype(np.int64)
+        C = self.bufs[op["sc"]]
+        offc = op["oc"] + (I * np.array(op["sC"], dtype=np.int64)[:, None]).sum(0)
+        s = np.zeros(I.shape[1], dtype=np.complex128)
+        for t in op["terms"]:
+            A = self.bufs[t["sa"]]
+            x = A[t["oa"] + (I * np.array(t["sA"], dtype=np.int64)[:, None]).sum(0)].astype(np.complex128)
+            if t["sb"] >= 0:
+                B = self.bufs[t["sb"]]
+                x = x * B[t["ob"] + (I * np.array(t["sB"], dtype=np.int64)[:, None]).sum(0)]
+            s += complex(t["cr"], t["ci"]) * x
+        if C.dtype == np.float64:
+            s = s.real
+        if op["acc"]:
+            C[offc] += s
+        else:
+            C[offc] = s
+
+    def _trace(self, op):
+        o, v, n = self.o, self.v, self.n
+        dij, l1, dai, dab = (self.bufs[k] for k in op["slots"])
+        rho = np.zeros((n, n), dtype=np.complex128)
+        rho[:o, :o] = dij[: o * o].reshape(o, o)
+        rho[:o, o:] = l1[: o * v].reshape(o, v)
+        rho[o:, :o] = dai[: v * o].reshape(v, o)
+        rho[o:, o:] = dab[: v * v].reshape(v, v)
+        mu = self.bufs[S_MU]
+        res = self.bufs[S_RES]
+        for k in range(op["n_mu"]):
+            res[k] = (mu[k * n * n:(k + 1) * n * n].reshape(n, n) * rho).sum()
