@@ -148,6 +148,25 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
                    double t0, double dt, int nsteps, int precs,
                    const tdcc_field* field, void* mu_traj, void* stream);
 
+/* Dipole expectation value like tdcc_dipole, but without allocating any
+   device memory and without a tdcc_system.  No counterpart in the reference
+   (its dipole_moment, CCSD_Helper.py:1066, allocates numpy temporaries).
+   For callers that cannot call cudaMalloc: code that runs inside someone
+   else's stream capture, plugins whose host framework owns all device
+   memory, processes that must not grow after start-up.
+   Scratch: a static device array of 3.375 MiB (221,184 complex128) that
+   every device loading the library keeps until exit; limits o <= 64 and
+   v <= 256 (larger: TDCC_ERR_LIMIT).  The first call on a device looks up
+   the array's device address (cudaGetSymbolAddress) with that device
+   current; make that first call before any stream capture.  All calls share
+   the one array: calls whose GPU work overlaps (different streams or
+   threads) race and give wrong results -- serialise them.  Inputs as in
+   tdcc_dipole; mu: device float64 [n_mu][n][n]; mu_out: device
+   complex128[n_mu].                                                       */
+int tdcc_dipole_noalloc(int o, int v, const void* t1, const void* t2, const void* l1,
+                        const void* l2, const double* mu, int n_mu, void* mu_out,
+                        void* stream);
+
 /* Writes a JSON description of the op list that computes (method, block)
    for sizes (o, v): buffer slots, and per op the GEMM mode groups / strides
    or the elementwise terms, plus whether the op runs once per RK4 step or
