@@ -116,6 +116,7 @@ struct Op {
   int dta = C64, dtb = C64, dtc = C64;
   GemmArgs g{};
   int backend = GB_FP64;
+  int tile = 0;            // FP64 tile shape index (kTiles)
   long long flops = 0;     // real flops of this contraction
   long long bytes = 0;     // compulsory bytes read + written
   // ADD
@@ -207,6 +208,11 @@ class Program {
   // mixed precision: which GEMMs go to the tensor-core backend
   void select_backend(int prec_mode, long long min_flops);
 };
+
+// FP64 contraction tile shapes (kernels.cu)
+constexpr int kNumTiles = 5;
+extern const int kTiles[kNumTiles][2];
+int choose_tile(long long M, long long N);
 
 // kernel launchers (kernels.cu)
 cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cudaStream_t st);

@@ -66,95 +66,109 @@ __device__ __forceinline__ void decomp(const ModeGroup& g, int l, long long& o0,
 
 // ---------------------------------------------------------------------------
 // FP64 contraction: C[m,n] (+)= alpha * sum_k A[m,k] B[k,n]
-// 64x64 output tile, K step 16, 256 threads, 4x4 outputs per thread (strided
-// by 16 so shared-memory reads are conflict free).  On GB300 the FP64 pipe
-// (~1.2 TFLOP/s) is the bound, so the tile favours occupancy over reuse.
+// BM x BN output tile, K step 16, 256 threads, TM x TN outputs per thread
+// (strided by BM/TM and BN/TN so shared-memory reads are conflict free).  On
+// GB300 the FP64 pipe (~1.2 TFLOP/s) is the bound, so the tile shape is
+// chosen per contraction to minimise padded (wasted) multiply-adds.
 // ---------------------------------------------------------------------------
-constexpr int GBM = 64, GBN = 64, GBK = 16;
+constexpr int GBK = 16;
 
-template <bool AC, bool BC, bool CC>
+template <bool AC, bool BC, bool CC, int BM, int BN, int TM, int TN>
 __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
+  static_assert((BM / TM) * (BN / TN) == 256, "256 threads");
+  static_assert(256 % BM == 0 && 256 % BN == 0, "tile rows divide the CTA");
   using TA = typename Elem<AC>::T;
   using TB = typename Elem<BC>::T;
-  __shared__ TA As[GBK][GBM];
-  __shared__ TB Bs[GBK][GBN];
+  constexpr int RX = BN / TN, RY = BM / TM;  // thread grid
+  constexpr int LA = BM * GBK / 256, LB = BN * GBK / 256;
+  __shared__ TA As[GBK][BM];
+  __shared__ TB Bs[GBK][BN];
 
   const int tid = threadIdx.x;
-  const int tx = tid & 15, ty = tid >> 4;
-  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+  const int tx = tid % RX, ty = tid / RX;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int kbeg = blockIdx.z * g.kchunk;
   const int kend = min(g.K, kbeg + g.kchunk);
 
   const TA* A = static_cast<const TA*>(g.A);
   const TB* B = static_cast<const TB*>(g.B);
 
-  // this thread's load row (A) / column (B) and its base offsets
-  const int lr = tid & 63;
-  const int lk = tid >> 6;  // 0..3
-  const int am = m0 + lr, bn = n0 + lr;
+  // this thread's load row (A) / column (B) and their base offsets
+  const int ar = tid % BM, ak0 = tid / BM;
+  const int br = tid % BN, bk0 = tid / BN;
+  const int am = m0 + ar, bn = n0 + br;
   long long aoff = 0, boff = 0, dummy;
   if (am < g.M) decomp(g.gm, am, aoff, dummy);
   if (bn < g.N) decomp(g.gn, bn, boff, dummy);
 
-  double2 acc[4][4];
+  double2 acc[TM][TN];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TM; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = cz();
+    for (int j = 0; j < TN; ++j) acc[i][j] = cz();
 
   for (int k0 = kbeg; k0 < kend; k0 += GBK) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int kk = lk + 4 * r;
+    for (int r = 0; r < LA; ++r) {
+      const int kk = ak0 + (256 / BM) * r;
       const int k = k0 + kk;
       TA av{};
-      TB bv{};
-      if (k < kend) {
+      if (k < kend && am < g.M) {
         long long ka, kb;
         decomp(g.gk, k, ka, kb);
-        if (am < g.M) av = A[aoff + ka];
-        if (bn < g.N) bv = B[boff + kb];
+        av = A[aoff + ka];
       }
-      As[kk][lr] = av;
-      Bs[kk][lr] = bv;
+      As[kk][ar] = av;
+    }
+#pragma unroll
+    for (int r = 0; r < LB; ++r) {
+      const int kk = bk0 + (256 / BN) * r;
+      const int k = k0 + kk;
+      TB bv{};
+      if (k < kend && bn < g.N) {
+        long long ka, kb;
+        decomp(g.gk, k, ka, kb);
+        bv = B[boff + kb];
+      }
+      Bs[kk][br] = bv;
     }
     __syncthreads();
 #pragma unroll 4
     for (int kk = 0; kk < GBK; ++kk) {
-      TA a[4];
-      TB b[4];
+      TA a[TM];
+      TB b[TN];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+      for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + RY * i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + RX * j];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) mac(acc[i][j], a[i], b[j]);
+        for (int j = 0; j < TN; ++j) mac(acc[i][j], a[i], b[j]);
     }
     __syncthreads();
   }
 
-  long long coffm[4], coffn[4];
+  long long coffm[TM], coffn[TN];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int m = m0 + ty + 16 * i;
+  for (int i = 0; i < TM; ++i) {
+    const int m = m0 + ty + RY * i;
     coffm[i] = 0;
     if (m < g.M) decomp(g.gm, m, dummy, coffm[i]);
   }
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int n = n0 + tx + 16 * j;
+  for (int j = 0; j < TN; ++j) {
+    const int n = n0 + tx + RX * j;
     coffn[j] = 0;
     if (n < g.N) decomp(g.gn, n, dummy, coffn[j]);
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int m = m0 + ty + 16 * i;
+  for (int i = 0; i < TM; ++i) {
+    const int m = m0 + ty + RY * i;
     if (m >= g.M) continue;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int n = n0 + tx + 16 * j;
+    for (int j = 0; j < TN; ++j) {
+      const int n = n0 + tx + RX * j;
       if (n >= g.N) continue;
       const double2 s = acc[i][j];
       const long long off = coffm[i] + coffn[j];
@@ -186,26 +200,57 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
   }
 }
 
+// tile shapes: {BM, BN}
+const int kTiles[kNumTiles][2] = {{64, 64}, {32, 64}, {64, 32}, {32, 32}, {16, 16}};
+
+int choose_tile(long long M, long long N) {
+  int best = 0;
+  double bc = 1e300;
+  for (int t = 0; t < kNumTiles; ++t) {
+    const long long bm = kTiles[t][0], bn = kTiles[t][1];
+    // padded multiply-adds, with a small penalty for less operand reuse
+    const double pen = (bm * bn >= 4096) ? 1.0 : (bm * bn >= 1024) ? 1.06 : 1.15;
+    const double cost = (double)((M + bm - 1) / bm * bm) * (double)((N + bn - 1) / bn * bn) * pen;
+    if (cost < bc) {
+      bc = cost;
+      best = t;
+    }
+  }
+  return best;
+}
+
+template <bool AC, bool BC, bool CC>
+static void launch_typed(int tile, dim3 grid, const GemmArgs& g, cudaStream_t st) {
+  switch (tile) {
+    case 0: gemm_f64_kernel<AC, BC, CC, 64, 64, 4, 4><<<grid, 256, 0, st>>>(g); break;
+    case 1: gemm_f64_kernel<AC, BC, CC, 32, 64, 2, 4><<<grid, 256, 0, st>>>(g); break;
+    case 2: gemm_f64_kernel<AC, BC, CC, 64, 32, 4, 2><<<grid, 256, 0, st>>>(g); break;
+    case 3: gemm_f64_kernel<AC, BC, CC, 32, 32, 2, 2><<<grid, 256, 0, st>>>(g); break;
+    default: gemm_f64_kernel<AC, BC, CC, 16, 16, 1, 1><<<grid, 256, 0, st>>>(g); break;
+  }
+}
+
 cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cudaStream_t st) {
   GemmArgs g = op.g;
   g.A = A;
   g.B = B;
   g.C = C;
-  const int gx = (g.N + GBN - 1) / GBN, gy = (g.M + GBM - 1) / GBM;
+  const int bm = kTiles[op.tile][0], bn = kTiles[op.tile][1];
+  const int gx = (g.N + bn - 1) / bn, gy = (g.M + bm - 1) / bm;
   const int gz = (g.K + g.kchunk - 1) / g.kchunk;
   dim3 grid(gx, gy, gz);
   if (gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
   const bool ac = op.dta == C64, bc = op.dtb == C64, cc = op.dtc == C64;
   if (ac && bc)
-    gemm_f64_kernel<true, true, true><<<grid, 256, 0, st>>>(g);
+    launch_typed<true, true, true>(op.tile, grid, g, st);
   else if (ac && !bc)
-    gemm_f64_kernel<true, false, true><<<grid, 256, 0, st>>>(g);
+    launch_typed<true, false, true>(op.tile, grid, g, st);
   else if (!ac && bc)
-    gemm_f64_kernel<false, true, true><<<grid, 256, 0, st>>>(g);
+    launch_typed<false, true, true>(op.tile, grid, g, st);
   else if (cc)
-    gemm_f64_kernel<false, false, true><<<grid, 256, 0, st>>>(g);
+    launch_typed<false, false, true>(op.tile, grid, g, st);
   else
-    gemm_f64_kernel<false, false, false><<<grid, 256, 0, st>>>(g);
+    launch_typed<false, false, false>(op.tile, grid, g, st);
   count_launch();
   return cudaGetLastError();
 }

@@ -218,8 +218,10 @@ void Program::ein(const char* spec, double ar, double ai, const View& A, const V
   g.ar = ar;
   g.ai = ai;
   g.acc = acc ? 1 : 0;
-  // split-K so that small output tiles still fill the 152 SMs
-  const long long tiles = ((M + 63) / 64) * ((N + 63) / 64);
+  // tile shape, then split-K so that few output tiles still fill the 152 SMs
+  op.tile = choose_tile(M, N);
+  const long long tiles = ((M + kTiles[op.tile][0] - 1) / kTiles[op.tile][0]) *
+                          ((N + kTiles[op.tile][1] - 1) / kTiles[op.tile][1]);
   long long splits = 1;
   if (tiles < 2 * 152 && K >= 64) {
     splits = (2 * 152 + tiles - 1) / tiles;

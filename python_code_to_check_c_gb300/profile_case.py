@@ -1,0 +1,42 @@
+"""Runs one right-hand side (or one RK4 step) of a named workload on the GPU,
+for profilers:  python -m python_code_to_check_c_gb300.profile_case
+    --workload o14_v58 --method CCSD --block T2 [--repeat 2] [--step]"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+import torch
+
+from . import _lib
+from .engine import CCEngine
+from .system import WORKLOADS, mp2_guess, synthetic_system
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--workload", default="o14_v58")
+    p.add_argument("--method", default="CCSD")
+    p.add_argument("--block", default="T2", choices=["T1", "T2", "L1", "L2"])
+    p.add_argument("--repeat", type=int, default=2)
+    p.add_argument("--step", action="store_true", help="one RK4 step instead of one RHS")
+    p.add_argument("--precision", default="fp64")
+    a = p.parse_args()
+    sysm = synthetic_system(**WORKLOADS[a.workload])
+    eng = CCEngine.from_system(sysm)
+    eng.set_precision(a.precision)
+    t2 = mp2_guess(sysm.tei(), sysm.eps(), sysm.o).astype(np.complex128)
+    t1 = np.full((sysm.o, sysm.v), 0.01 + 0.005j)
+    st = (t1, t2, t1.copy(), t2.copy())
+    blk = {"T1": 0, "T2": 1, "L1": 2, "L2": 3}[a.block]
+    for _ in range(a.repeat):
+        if a.step:
+            eng.rk4_step(a.method, st, 0.0, 0.005, _lib.make_field("sin", 0.002, 0.923))
+        else:
+            eng.rhs(a.method, blk, *st, F=sysm.fock)
+    torch.cuda.synchronize()
+    print("ok", a.workload, a.method, a.block, "step" if a.step else "rhs")
+
+
+if __name__ == "__main__":
+    main()
