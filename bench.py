@@ -204,6 +204,26 @@ def run_ours(args, rank, world, local_rank):
         t_max = float(tt.item())
     value = world * args.steps / (t_max / 1e3)
     finite = bool(torch.isfinite(torch.view_as_real(traj)).all().item())
+    eng.check_errors()
+
+    # ---- the plain FP64 form on the same start state (ratio and |d mu|) ----
+    fp64 = None
+    if prec == "mixed":
+        k64 = max(1, min(args.steps, 30))
+        eng.set_precision("fp64")
+        eng.propagate(args.method, dst, 0.0, DT, 3, field)
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record()
+        _, traj64 = eng.propagate(args.method, dst, 0.0, DT, k64, field)
+        g1.record()
+        torch.cuda.synchronize()
+        v64 = k64 / (g0.elapsed_time(g1) / 1e3)
+        dmu = float((traj[:k64] - traj64).abs().max().item())
+        fp64 = {"value": world * v64, "steps": k64, "mixed_over_fp64": value / (world * v64),
+                "max_dmu_vs_fp64_au": dmu, "slices": 5}
+        eng.set_precision("mixed", 5)
+        eng.propagate(args.method, dst, 0.0, DT, 1, field)
 
     # ---- end-to-end through the C ABI with host buffers ----
     ke = max(1, min(args.e2e_steps, args.steps))
@@ -289,6 +309,7 @@ def run_ours(args, rank, world, local_rank):
                    "l2": f"per-step working set {ws / 2**20:.0f} MiB workspace + "
                          f"{sysm.n ** 4 * 8 / 2**20:.0f} MiB integrals (> 129 MB L2), no flush"},
         "roofline": roof, "kernel_breakdown": breakdown, "cpu_baseline": cpu, "e2e": e2e,
+        "fp64_form": fp64,
         "gpu_launches": launches, "launches_per_step": launches / args.steps, "clocks": clk.summary(),
         "finite": finite,
     }

@@ -101,6 +101,11 @@ int tdcc_system_destroy(tdcc_system s);
    the number of BF16 slices per operand (3..7).                           */
 int tdcc_set_precision(tdcc_system s, int mode, int slices);
 
+/* Synchronises the device and reports TDCC_ERR_CUDA if a kernel of this
+   system recorded an error (a tensor-core kernel whose bounded wait
+   expired); clears the flag.                                              */
+int tdcc_check_errors(tdcc_system s);
+
 /* Bytes of device workspace currently held by the system.                 */
 long long tdcc_workspace_bytes(tdcc_system s);
 

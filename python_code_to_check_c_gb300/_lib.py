@@ -62,6 +62,7 @@ SIGNATURES = {
     "tdcc_system_destroy": (_i, [_vp]),
     "tdcc_set_precision": (_i, [_vp, _i, _i]),
     "tdcc_workspace_bytes": (_ll, [_vp]),
+    "tdcc_check_errors": (_i, [_vp]),
     "tdcc_rhs": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tdcc_dipole": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tdcc_rk4_step": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _i,

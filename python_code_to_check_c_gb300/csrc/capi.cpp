@@ -30,7 +30,16 @@ bool tc_available();
 struct ProgInst {
   std::unique_ptr<Program> prog;
   std::vector<void*> bases;
+  std::vector<void*> owned;  // this program's workspace allocations
+  long long bytes = 0;
+  ~ProgInst() {
+    for (void* p : owned) cudaFree(p);
+  }
 };
+
+// contractions with at least this many multiply-adds (and K >= 64) use the
+// tensor-core slice products in the mixed-precision mode
+constexpr long long kTcMinMacs = 1LL << 21;
 
 }  // namespace tdcc
 
@@ -123,11 +132,12 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
     build_l1_cc2(p);
   else
     build_l2_cc2(p, p.ones("ones_v", s->dims.v));
+  p.select_backend(s->prec_mode, kTcMinMacs, s->slices);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
-  p.select_backend(s->prec_mode, 1LL << 40);
   pi->bases.assign(p.slots.size(), nullptr);
-  s->ws_bytes += p.allocate(pi->bases, s->owned);
+  pi->bytes = p.allocate(pi->bases, pi->owned);
+  s->ws_bytes += pi->bytes;
   bind_fixed(s, pi->bases);
   slot = std::move(pi);
   return *slot;
@@ -344,11 +354,45 @@ int tdcc_set_precision(tdcc_system s, int mode, int slices) {
   if (mode == TDCC_PREC_MIXED && !tc_available())
     return fail(TDCC_ERR_STATE, "tensor-core backend not built into this library");
   if (mode == TDCC_PREC_MIXED && (slices < 3 || slices > 7)) return fail(TDCC_ERR_ARG, "slices must be 3..7");
-  s->prec_mode = mode;
-  s->slices = slices;
+  if (mode == TDCC_PREC_FP64) slices = s->slices;
+  if (mode == s->prec_mode && slices == s->slices) return TDCC_OK;
+  // programs are rebuilt (and their workspace reallocated) on next use
+  cudaDeviceSynchronize();
   for (auto& mrow : s->rhs)
     for (auto& pi : mrow)
-      if (pi) pi->prog->select_backend(mode, 1LL << 40);
+      if (pi) {
+        s->ws_bytes -= pi->bytes;
+        pi.reset();
+      }
+  for (auto& g : s->gexec)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  s->prec_mode = mode;
+  s->slices = slices;
+  return TDCC_OK;
+}
+
+int tdcc_check_errors(tdcc_system s) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  const cudaError_t ce = cudaDeviceSynchronize();
+  if (ce != cudaSuccess) return fail(TDCC_ERR_CUDA, std::string("device error: ") + cudaGetErrorString(ce));
+  for (int m = 0; m < 2; ++m)
+    for (int b = 0; b < 4; ++b) {
+      auto& pi = s->rhs[m][b];
+      if (!pi || pi->prog->err_slot < 0) continue;
+      int flag = 0;
+      void* p = pi->bases[pi->prog->err_slot];
+      if (cudaMemcpy(&flag, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(TDCC_ERR_CUDA, "reading the tensor-core error flag failed");
+      if (flag) {
+        const int zero = 0;
+        cudaMemcpy(p, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(TDCC_ERR_CUDA, "tensor-core kernel in " + pi->prog->name + " gave up waiting (code " +
+                                       std::to_string(flag) + ")");
+      }
+    }
   return TDCC_OK;
 }
 

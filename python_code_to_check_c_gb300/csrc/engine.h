@@ -11,7 +11,9 @@
 
 namespace tdcc {
 
-enum DType : int { R64 = 0, C64 = 1 };
+enum DType : int { R64 = 0, C64 = 1, U8 = 2 };
+
+inline long long elem_bytes(int dt) { return dt == C64 ? 16 : dt == R64 ? 8 : 1; }
 
 // ---------------------------------------------------------------------------
 // Kernel argument blocks (passed by value to the kernels)
@@ -103,7 +105,38 @@ struct Term {
   View B;  // slot -1: absent
 };
 
-enum OpKind { OP_GEMM = 0, OP_ADD = 1, OP_TRACE = 2 };
+enum OpKind { OP_GEMM = 0, OP_ADD = 1, OP_TRACE = 2, OP_PACK = 3, OP_TCGEMM = 4 };
+
+// Tensor-core backend argument blocks (gemm_tc.cu).
+struct PackArgs {
+  const void* src;   // FP64 tensor (real or interleaved complex)
+  int cplx;
+  ModeGroup gr;      // row modes, strides in s0 (elements of src)
+  ModeGroup gk;      // K modes, strides in s0
+  int rows;          // logical rows (M or N)
+  int K;
+  int rows_pad;      // packed rows (x2 for complex), multiple of the tile
+  int K_pad;         // multiple of the K tile
+  int S;             // slices
+  void* out;         // [S][rows_pad][K_pad] BF16
+  int* exps;         // [rows_pad]
+};
+
+struct TcArgs {
+  int M, N;                 // logical output extents
+  int rowsA_pad, rowsB_pad; // packed rows
+  int kblocks, kb_per_split;
+  int S;
+  int tmem_cols;
+  int ac, bc, cc;           // A, B, C complex?
+  const int* expA;
+  const int* expB;
+  ModeGroup gmC, gnC;       // output offsets: strides in s0
+  void* C;
+  double ar, ai;
+  int acc, atomic;
+  int* err;
+};
 
 enum GemmBackend { GB_FP64 = 0, GB_TC = 1 };
 
@@ -128,6 +161,14 @@ struct Op {
   // TRACE: res[k] = sum over 4 density blocks of mu_k * rho (see kernels)
   int tr_slots[4];
   int tr_n_mu = 0;
+  // PACK: operand slot/offset/type -> packed slot (exponents at pk_exp_off bytes)
+  PackArgs pk{};
+  int pk_src = -1, pk_dt = R64, pk_dst = -1;
+  long long pk_off = 0, pk_exp_off = 0;
+  // TCGEMM: packed A / B slots, output C, error-flag slot
+  TcArgs tc{};
+  int tc_pa = -1, tc_pb = -1, tc_err = -1;
+  long long tc_expa_off = 0, tc_expb_off = 0;
   // dependency analysis
   std::vector<int> reads;
   int write = -1;
@@ -206,7 +247,11 @@ class Program {
                   std::vector<Timed>* timed = nullptr) const;
 
   // mixed precision: which GEMMs go to the tensor-core backend
-  void select_backend(int prec_mode, long long min_flops);
+  // (before analyse/allocate) rewrites every contraction with at least
+  // `min_macs` multiply-adds and K >= 64 into pack A, pack B and a
+  // tensor-core slice product with `slices` BF16 slices per operand
+  void select_backend(int prec_mode, long long min_macs, int slices);
+  int err_slot = -1;  // U8 slot holding the tensor-core kernels' error flag
 };
 
 // FP64 contraction tile shapes (kernels.cu)
@@ -216,6 +261,9 @@ int choose_tile(long long M, long long N);
 
 // kernel launchers (kernels.cu)
 cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cudaStream_t st);
+cudaError_t launch_pack(const PackArgs& p, cudaStream_t st);
+cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st);
+bool tc_available();
 cudaError_t launch_add(const AddArgs& a, cudaStream_t st);
 cudaError_t launch_trace(int n, int o, int n_mu, const double* mu, const void* dij,
                          const void* l1, const void* dai, const void* dab, void* res,

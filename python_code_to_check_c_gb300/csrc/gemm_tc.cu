@@ -1,9 +1,484 @@
-// Tensor-core (tcgen05) backend for the large contractions of the mixed
-// precision mode.
+// Tensor-core backend of the mixed-precision mode: FP64 contractions
+// computed as exact integer products of BF16 slices on tcgen05.
+//
+// Operand packing (pack_kernel): each row of A (an M x K view) and each
+// column of B (a K x N view) is scaled by 2^-e with e the binary exponent of
+// its largest magnitude, then cut into S slices of 7 bits,
+//     x * 2^-e = sum_s q_s 2^(-7s),  q_s integers, |q_1| <= 128, |q_s| <= 64,
+// each exactly representable in BF16.  Complex operands contribute two packed
+// rows (real, imaginary) per logical row.  Packed layout: [S][rows][K] BF16,
+// K contiguous (K-major for UMMA), rows and K zero-padded to the tile sizes.
+//
+// Products (ozaki_kernel): for every pair (s, t) with s + t <= S + 1 the
+// slice product A_s B_t^T is accumulated by tcgen05.mma (kind::f16, BF16
+// inputs, FP32 accumulate in TMEM) into the accumulator of its level
+// L = s + t.  |q_s q_t| <= 2^14, so FP32 sums of up to 1024 products are
+// exact; after every 1024-wide K chunk the epilogue warps drain the TMEM
+// accumulators into FP64 registers with their 2^(-7L) weights.  The final
+// value is scaled back by 2^(e_row + e_col); real/imaginary rows of complex
+// operands are combined with a lane-pair shuffle and written through the
+// same strided output decoder as the FP64 kernel.
+//
+// Pipeline: 6 warps.  Warp 0 issues TMA loads (SWIZZLE_128B) into an
+// 8-stage shared-memory ring, one (A_s, B_s) slice pair per stage; warp 1
+// owns TMEM and issues the MMAs from one thread; warps 2-5 drain TMEM.
+// Every wait has an iteration limit: on expiry the kernel records an error
+// code, stops issuing work, waits (bounded) for its own operations and frees
+// TMEM before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
 #include "engine.h"
+#include "gemm_tc.h"
 
 namespace tdcc {
 
-bool tc_available() { return false; }
+// ---------------------------------------------------------------------------
+// packing
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void decomp_tc(const ModeGroup& g, int l, long long& o0) {
+  o0 = 0;
+#pragma unroll
+  for (int q = kMaxModes - 1; q >= 0; --q) {
+    if (q < g.n) {
+      const int d = g.dim[q];
+      const int r = l % d;
+      l /= d;
+      o0 += (long long)r * g.s0[q];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= p.rows_pad) return;
+  const int pr = warp;
+  const int m = p.cplx ? (pr >> 1) : pr;
+  const int part = p.cplx ? (pr & 1) : 0;
+  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+  const size_t plane = (size_t)p.rows_pad * p.K_pad;
+  if (m >= p.rows) {
+    for (int k = lane; k < p.K_pad; k += 32)
+      for (int s = 0; s < p.S; ++s) out[s * plane + (size_t)pr * p.K_pad + k] = __float2bfloat16_rn(0.f);
+    if (lane == 0) p.exps[pr] = 0;
+    return;
+  }
+  long long roff;
+  decomp_tc(p.gr, m, roff);
+  const double* src = static_cast<const double*>(p.src);
+  auto load = [&](int k) -> double {
+    long long ko;
+    decomp_tc(p.gk, k, ko);
+    const long long e = roff + ko;
+    return p.cplx ? src[2 * e + part] : src[e];
+  };
+  double mx = 0.0;
+  for (int k = lane; k < p.K; k += 32) mx = fmax(mx, fabs(load(k)));
+  for (int d = 16; d > 0; d >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
+  for (int k = lane; k < p.K_pad; k += 32) {
+    double r = k < p.K ? ldexp(load(k), -e) : 0.0;
+    for (int s = 0; s < p.S; ++s) {
+      const double q = rint(ldexp(r, 7 * (s + 1)));
+      r -= ldexp(q, -7 * (s + 1));
+      out[s * plane + (size_t)pr * p.K_pad + k] = __float2bfloat16_rn((float)q);
+    }
+  }
+  if (lane == 0) p.exps[pr] = e;
+}
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t c) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(c));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false after `limit` polls (each poll may suspend briefly)
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (mbar_try(a, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma3d(uint32_t dst, const CUtensorMap* tm, int x, int y, int z, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          dst),
+      "l"((uint64_t)tm), "r"(x), "r"(y), "r"(z), "r"(mbar)
+      : "memory");
+}
+// UMMA shared-memory descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+// instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+      "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// ---------------------------------------------------------------------------
+// slice-product kernel
+// ---------------------------------------------------------------------------
+constexpr int kWaitLimit = 1 << 22;
+
+struct TcShared {
+  uint64_t full[TC_STAGES];
+  uint64_t empty[TC_STAGES];
+  uint64_t accfull, accempty, done;
+  uint32_t tmem;
+  volatile int abort;  // set by any role on an expired wait; polled by all
+};
+
+__device__ __forceinline__ void fail(TcShared* sh, int* err, int code) {
+  sh->abort = 1;
+  atomicCAS(err, 0, code);
+}
+
+template <bool AC, bool BC>
+__global__ void __launch_bounds__(192, 1)
+    ozaki_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs g) {
+  extern __shared__ uint8_t smraw[];
+  uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  uint8_t* stA = sm;                                   // TC_STAGES x 16 KB
+  uint8_t* stB = sm + TC_STAGES * TC_A_BYTES;          // TC_STAGES x 8 KB
+  TcShared* sh = (TcShared*)(stB + TC_STAGES * TC_B_BYTES);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = g.S;
+  const int ncols = g.tmem_cols;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < TC_STAGES; ++i) {
+      mbar_init(smem_u32(&sh->full[i]), 1);
+      mbar_init(smem_u32(&sh->empty[i]), 1);
+    }
+    mbar_init(smem_u32(&sh->accfull), 1);
+    mbar_init(smem_u32(&sh->accempty), 128);
+    mbar_init(smem_u32(&sh->done), 1);
+    sh->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    asm volatile("fence.proxy.async.shared::cta;");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = sh->tmem;
+
+  const int mt = blockIdx.y, nt = blockIdx.x;
+  const int kb0 = blockIdx.z * g.kb_per_split;
+  const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
+  const int nkb = kb1 - kb0;
+  const int nchunks = (nkb + TC_CHUNK_KB - 1) / TC_CHUNK_KB;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0;
+      for (int kb = kb0; kb < kb1 && !sh->abort; ++kb)
+        for (int s = 0; s < S && !sh->abort; ++s, ++it) {
+          const int st = it % TC_STAGES;
+          const uint32_t ph = (uint32_t)((it / TC_STAGES) & 1);
+          if (!mbar_wait(smem_u32(&sh->empty[st]), ph ^ 1u, kWaitLimit)) {
+            fail(sh, g.err, 1);
+            break;
+          }
+          const uint32_t fb = smem_u32(&sh->full[st]);
+          mbar_expect_tx(fb, TC_A_BYTES + TC_B_BYTES);
+          tma3d(smem_u32(stA + st * TC_A_BYTES), &tmA, kb * TC_BK, mt * TC_BM, s, fb);
+          tma3d(smem_u32(stB + st * TC_B_BYTES), &tmB, kb * TC_BK, nt * TC_BN, s, fb);
+        }
+      // drain: every issued load must land before the CTA exits
+      const int issued = it;
+      for (int j = (issued > TC_STAGES ? issued - TC_STAGES : 0); j < issued; ++j)
+        mbar_wait(smem_u32(&sh->full[j % TC_STAGES]), (uint32_t)((j / TC_STAGES) & 1), kWaitLimit);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t id = idesc_bf16(TC_BM, TC_BN);
+      int it = 0;
+      for (int c = 0; c < nchunks && !sh->abort; ++c) {
+        if (c > 0 && !mbar_wait(smem_u32(&sh->accempty), (uint32_t)((c - 1) & 1), kWaitLimit)) {
+          fail(sh, g.err, 2);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const int kbs = kb0 + c * TC_CHUNK_KB, kbe = min(kb1, kbs + TC_CHUNK_KB);
+        bool first = true;
+        for (int kb = kbs; kb < kbe && !sh->abort; ++kb, it += S) {
+          bool ok = true;
+          for (int s = 0; s < S; ++s) {
+            const int j = it + s;
+            if (!mbar_wait(smem_u32(&sh->full[j % TC_STAGES]), (uint32_t)((j / TC_STAGES) & 1), kWaitLimit)) {
+              ok = false;
+              break;
+            }
+          }
+          if (!ok) {
+            fail(sh, g.err, 3);
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          for (int L = 2; L <= S + 1; ++L) {
+            const uint32_t dacc = tmem + (uint32_t)((L - 2) * TC_BN);
+            int np = 0;
+            for (int s = 1; s < L; ++s) {
+              const int t = L - s;
+              if (s > S || t > S) continue;
+              const int sa = (it + s - 1) % TC_STAGES, sb = (it + t - 1) % TC_STAGES;
+              const uint64_t da = sdesc(smem_u32(stA + sa * TC_A_BYTES));
+              const uint64_t db = sdesc(smem_u32(stB + sb * TC_B_BYTES));
+#pragma unroll
+              for (int k = 0; k < TC_BK / 16; ++k) {
+                const uint32_t accf = (first && np == 0 && k == 0) ? 0u : 1u;
+                umma(dacc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), id, accf);
+              }
+              ++np;
+            }
+          }
+          first = false;
+          for (int s = 0; s < S; ++s) umma_commit(smem_u32(&sh->empty[(it + s) % TC_STAGES]));
+        }
+        umma_commit(smem_u32(&sh->accfull));
+      }
+      // all issued MMAs complete before TMEM is released
+      umma_commit(smem_u32(&sh->done));
+      mbar_wait(smem_u32(&sh->done), 0, kWaitLimit);
+    }
+  } else {
+    // ---------------- epilogue (warps 2..5) ----------------
+    const int q = warp & 3;             // TMEM lane quarter this warp may access
+    const int row = q * 32 + lane;      // tile row == TMEM lane
+    double acc[TC_BN];
+#pragma unroll
+    for (int j = 0; j < TC_BN; ++j) acc[j] = 0.0;
+    for (int c = 0; c < nchunks; ++c) {
+      // warp-uniform decisions: tcgen05.ld and the shuffles below are collective
+      if (__any_sync(0xffffffffu, sh->abort != 0)) break;
+      const bool got = mbar_wait(smem_u32(&sh->accfull), (uint32_t)(c & 1), kWaitLimit);
+      if (!__all_sync(0xffffffffu, got)) {
+        fail(sh, g.err, 4);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      for (int L = 2; L <= S + 1; ++L) {
+        const double w = ldexp(1.0, -7 * L);
+#pragma unroll
+        for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((L - 2) * TC_BN + j0), v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) acc[j0 + j] = fma((double)v[j], w, acc[j0 + j]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mbar_arrive(smem_u32(&sh->accempty));
+    }
+    if (!__any_sync(0xffffffffu, sh->abort != 0)) {
+      // scale back and write
+      const int prow = mt * TC_BM + row;          // packed row of A
+      const int ea = prow < g.rowsA_pad ? g.expA[prow] : 0;
+#pragma unroll
+      for (int j = 0; j < TC_BN; ++j) {
+        const int pcol = nt * TC_BN + j;
+        const int eb = g.expB[pcol];
+        acc[j] = ldexp(acc[j], ea + eb);
+      }
+      const int m = AC ? (prow >> 1) : prow;
+      const bool odd = AC && (lane & 1);
+      long long coffm = 0;
+      if (m < g.M) decomp_tc(g.gmC, m, coffm);
+      double2* C = static_cast<double2*>(g.C);
+      constexpr int ncol_log = BC ? TC_BN / 2 : TC_BN;  // logical output columns in this tile
+#pragma unroll
+      for (int jj = 0; jj < ncol_log; ++jj) {
+        double re, im;
+        if constexpr (BC) {
+          const double x0 = acc[2 * jj], x1 = acc[2 * jj + 1];
+          if constexpr (AC) {
+            const double p0 = __shfl_xor_sync(0xffffffffu, x0, 1);
+            const double p1 = __shfl_xor_sync(0xffffffffu, x1, 1);
+            // even lane: (rr, ri) own, (ir, ii) partner; odd lane the reverse
+            const double rr = odd ? p0 : x0, ri = odd ? p1 : x1, ir = odd ? x0 : p0, ii = odd ? x1 : p1;
+            re = rr - ii;
+            im = ri + ir;
+          } else {
+            re = x0;
+            im = x1;
+          }
+        } else {
+          const double x = acc[jj];
+          if constexpr (AC) {
+            const double p = __shfl_xor_sync(0xffffffffu, x, 1);
+            re = odd ? p : x;
+            im = odd ? x : p;
+          } else {
+            re = x;
+            im = 0.0;
+          }
+        }
+        // with complex A the two lanes of a pair hold the same output: split columns
+        if (AC && ((jj & 1) != (lane & 1))) continue;
+        const int n = nt * ncol_log + jj;
+        if (m >= g.M || n >= g.N) continue;
+        long long coffn;
+        decomp_tc(g.gnC, n, coffn);
+        const long long off = coffm + coffn;
+        const double vr = g.ar * re - g.ai * im, vi = g.ar * im + g.ai * re;
+        if (g.cc) {
+          if (g.atomic) {
+            atomicAdd(&C[off].x, vr);
+            atomicAdd(&C[off].y, vi);
+          } else if (g.acc) {
+            double2 cv = C[off];
+            cv.x += vr;
+            cv.y += vi;
+            C[off] = cv;
+          } else {
+            C[off] = make_double2(vr, vi);
+          }
+        } else {
+          double* Cr = static_cast<double*>(g.C);
+          if (g.atomic)
+            atomicAdd(&Cr[off], vr);
+          else if (g.acc)
+            Cr[off] += vr;
+          else
+            Cr[off] = vr;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+bool tc_available() { return true; }
+
+static PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        !p)
+      throw std::runtime_error("cuTensorMapEncodeTiled unavailable");
+    fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// [S][rows_pad][K_pad] BF16, box = (64 K, box_rows rows, 1 slice)
+static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, int box_rows) {
+  CUtensorMap m;
+  cuuint64_t dims[3] = {(cuuint64_t)K_pad, (cuuint64_t)rows_pad, (cuuint64_t)S};
+  cuuint64_t strides[2] = {(cuuint64_t)K_pad * 2, (cuuint64_t)K_pad * 2 * rows_pad};
+  cuuint32_t box[3] = {TC_BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  const CUresult r = encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
+                               es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
+cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
+  const long long threads = (long long)p.rows_pad * 32;
+  pack_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(p);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(ozaki_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         TC_SMEM_BYTES);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ozaki_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               TC_SMEM_BYTES);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ozaki_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               TC_SMEM_BYTES);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ozaki_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               TC_SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const CUtensorMap ma = slice_map(packA, a.S, a.rowsA_pad, a.kblocks * TC_BK, TC_BM);
+  const CUtensorMap mb = slice_map(packB, a.S, a.rowsB_pad, a.kblocks * TC_BK, TC_BN);
+  dim3 grid(a.rowsB_pad / TC_BN, a.rowsA_pad / TC_BM, (a.kblocks + a.kb_per_split - 1) / a.kb_per_split);
+  if (a.ac && a.bc)
+    ozaki_kernel<true, true><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+  else if (a.ac)
+    ozaki_kernel<true, false><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+  else if (a.bc)
+    ozaki_kernel<false, true><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+  else
+    ozaki_kernel<false, false><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+  count_launch();
+  return cudaGetLastError();
+}
 
 }  // namespace tdcc

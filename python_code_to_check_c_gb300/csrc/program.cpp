@@ -383,7 +383,7 @@ long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned
   long long bytes = 0;
   if (bases.size() < slots.size()) bases.resize(slots.size(), nullptr);
   for (size_t i = kNumFixedSlots; i < slots.size(); ++i) {
-    const size_t b = (size_t)slots[i].numel * (slots[i].dt == C64 ? 16 : 8);
+    const size_t b = (size_t)slots[i].numel * (size_t)elem_bytes(slots[i].dt);
     void* p = nullptr;
     if (cudaMalloc(&p, b) != cudaSuccess) {
       cudaGetLastError();
@@ -402,7 +402,7 @@ long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned
 
 static inline const void* at(const std::vector<void*>& b, int slot, long long off, int dt) {
   const char* p = static_cast<const char*>(b[slot]);
-  return p + off * (dt == C64 ? 16 : 8);
+  return p + off * elem_bytes(dt);
 }
 
 cudaError_t Program::run(const std::vector<void*>& bases, cudaStream_t st, Phase ph,
@@ -434,6 +434,22 @@ cudaError_t Program::run(const std::vector<void*>& bases, cudaStream_t st, Phase
       e = launch_trace(dims.n, dims.o, op.tr_n_mu, static_cast<const double*>(bases[S_MU]),
                        bases[op.tr_slots[0]], bases[op.tr_slots[1]], bases[op.tr_slots[2]],
                        bases[op.tr_slots[3]], bases[S_RES], st);
+    } else if (op.kind == OP_PACK) {
+      PackArgs p = op.pk;
+      p.src = at(bases, op.pk_src, op.pk_off, op.pk_dt);
+      char* dst = static_cast<char*>(bases[op.pk_dst]);
+      p.out = dst;
+      p.exps = reinterpret_cast<int*>(dst + op.pk_exp_off);
+      e = launch_pack(p, st);
+    } else if (op.kind == OP_TCGEMM) {
+      TcArgs a = op.tc;
+      const char* pa = static_cast<const char*>(bases[op.tc_pa]);
+      const char* pb = static_cast<const char*>(bases[op.tc_pb]);
+      a.expA = reinterpret_cast<const int*>(pa + op.tc_expa_off);
+      a.expB = reinterpret_cast<const int*>(pb + op.tc_expb_off);
+      a.C = const_cast<void*>(at(bases, op.sc, op.oc, op.dtc));
+      a.err = static_cast<int*>(bases[op.tc_err]);
+      e = launch_ozaki(a, pa, pb, st);
     }
     if (timed) {
       cudaEventRecord(tm.b, st);
@@ -447,9 +463,171 @@ cudaError_t Program::run(const std::vector<void*>& bases, cudaStream_t st, Phase
   return cudaSuccess;
 }
 
-void Program::select_backend(int prec_mode, long long min_flops) {
-  for (auto& op : ops)
-    if (op.kind == OP_GEMM) op.backend = (prec_mode == 1 && op.flops >= min_flops) ? GB_TC : GB_FP64;
+static long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
+
+void Program::select_backend(int prec_mode, long long min_macs, int S) {
+  if (prec_mode != 1) return;
+  if (S < 1 || S > 7) throw std::runtime_error("slices must be 1..7");
+  constexpr int BM = 128, BN = 64, BK = 64;  // tensor-core tile (gemm_tc.h)
+  std::vector<Op> out;
+  out.reserve(ops.size() * 2);
+  for (auto& op : ops) {
+    if (op.kind != OP_GEMM) {
+      out.push_back(op);
+      continue;
+    }
+    const long long M = op.g.M, N = op.g.N, K = op.g.K;
+    if (M * N * K < min_macs || K < BK) {
+      out.push_back(op);
+      continue;
+    }
+    if (err_slot < 0) {
+      int d1[1] = {256};
+      View e = ws_dims("tc_err", 1, d1, U8);
+      slots[e.slot].init.assign(32, 0.0);
+      err_slot = e.slot;
+    }
+    const bool ac = op.dta == C64, bc = op.dtb == C64;
+    const long long rA = rup(M * (ac ? 2 : 1), BM), rB = rup(N * (bc ? 2 : 1), BN), Kp = rup(K, BK);
+    auto packed_slot = [&](const std::string& nm, long long rows, long long& exp_off) {
+      exp_off = rup((long long)S * rows * Kp * 2, 256);
+      int d1[1] = {(int)0};
+      const long long bytes = exp_off + rup(rows * 4, 256);
+      if (bytes > (1LL << 31) - 1) {
+        // store as R64 elements to keep the extent in an int
+        d1[0] = (int)((bytes + 7) / 8);
+        return ws_dims(nm, 1, d1, R64).slot;
+      }
+      d1[0] = (int)bytes;
+      return ws_dims(nm, 1, d1, U8).slot;
+    };
+    Op pa, pb, t;
+    pa.kind = pb.kind = OP_PACK;
+    pa.tag = op.tag + ":packA";
+    pb.tag = op.tag + ":packB";
+    pa.pk_dst = packed_slot(op.tag + ":packA", rA, pa.pk_exp_off);
+    pb.pk_dst = packed_slot(op.tag + ":packB", rB, pb.pk_exp_off);
+    // A: rows = M modes (strides g.gm.s0), K modes strides g.gk.s0
+    pa.pk = PackArgs{};
+    pa.pk.cplx = ac;
+    pa.pk.gr = op.g.gm;
+    pa.pk.gk = op.g.gk;
+    pa.pk.rows = (int)M;
+    pa.pk.K = (int)K;
+    pa.pk.rows_pad = (int)rA;
+    pa.pk.K_pad = (int)Kp;
+    pa.pk.S = S;
+    pa.pk_src = op.sa;
+    pa.pk_off = op.oa;
+    pa.pk_dt = op.dta;
+    pa.reads = {op.sa};
+    pa.write = pa.pk_dst;
+    pa.bytes = M * K * elem_bytes(op.dta) + (long long)S * rA * Kp * 2;
+    // B: rows = N modes (strides g.gn.s0), K modes strides g.gk.s1
+    pb.pk = PackArgs{};
+    pb.pk.cplx = bc;
+    pb.pk.gr = op.g.gn;
+    pb.pk.gk = op.g.gk;
+    for (int i = 0; i < kMaxModes; ++i) pb.pk.gk.s0[i] = op.g.gk.s1[i];
+    pb.pk.rows = (int)N;
+    pb.pk.K = (int)K;
+    pb.pk.rows_pad = (int)rB;
+    pb.pk.K_pad = (int)Kp;
+    pb.pk.S = S;
+    pb.pk_src = op.sb;
+    pb.pk_off = op.ob;
+    pb.pk_dt = op.dtb;
+    pb.reads = {op.sb};
+    pb.write = pb.pk_dst;
+    pb.bytes = N * K * elem_bytes(op.dtb) + (long long)S * rB * Kp * 2;
+    // slice product
+    t.kind = OP_TCGEMM;
+    t.tag = op.tag;
+    t.backend = GB_TC;
+    t.flops = op.flops;
+    t.sc = op.sc;
+    t.oc = op.oc;
+    t.dtc = op.dtc;
+    t.tc_pa = pa.pk_dst;
+    t.tc_pb = pb.pk_dst;
+    t.tc_err = err_slot;
+    t.tc_expa_off = pa.pk_exp_off;
+    t.tc_expb_off = pb.pk_exp_off;
+    TcArgs& a = t.tc;
+    a = TcArgs{};
+    a.M = (int)M;
+    a.N = (int)N;
+    a.rowsA_pad = (int)rA;
+    a.rowsB_pad = (int)rB;
+    a.kblocks = (int)(Kp / BK);
+    a.S = S;
+    int cols = 32;
+    while (cols < S * BN) cols *= 2;
+    a.tmem_cols = cols;
+    a.ac = ac;
+    a.bc = bc;
+    a.cc = op.dtc == C64;
+    a.gmC = op.g.gm;
+    a.gnC = op.g.gn;
+    for (int i = 0; i < kMaxModes; ++i) {
+      a.gmC.s0[i] = op.g.gm.s1[i];
+      a.gnC.s0[i] = op.g.gn.s1[i];
+    }
+    a.ar = op.g.ar;
+    a.ai = op.g.ai;
+    a.acc = op.g.acc;
+    // split K so that few output tiles still occupy the SMs
+    const long long ctas = (rB / BN) * (rA / BM);
+    long long splits = 1;
+    if (ctas < 152 && a.kblocks >= 4) {
+      splits = std::min<long long>((152 + ctas - 1) / ctas, a.kblocks / 2);
+      splits = std::max<long long>(splits, 1);
+    }
+    a.kb_per_split = (int)((a.kblocks + splits - 1) / splits);
+    splits = (a.kblocks + a.kb_per_split - 1) / a.kb_per_split;
+    a.atomic = splits > 1 ? 1 : 0;
+    t.bytes = (long long)S * (rA + rB) * Kp * 2 + M * N * elem_bytes(op.dtc);
+    t.reads = {pa.pk_dst, pb.pk_dst};
+    if (a.acc || a.atomic) t.reads.push_back(op.sc);
+    t.write = op.sc;
+    out.push_back(pa);
+    out.push_back(pb);
+    if (a.atomic && !a.acc) {
+      // zero the output first: its modes are the M and N groups (strides s1)
+      Op z;
+      z.kind = OP_ADD;
+      z.tag = op.tag + ":zero";
+      AddArgs& za = z.a;
+      memset(&za, 0, sizeof(za));
+      int nd = 0;
+      long long dims[6], strd[6];
+      for (int i = 0; i < op.g.gm.n; ++i, ++nd) {
+        dims[nd] = op.g.gm.dim[i];
+        strd[nd] = op.g.gm.s1[i];
+      }
+      for (int i = 0; i < op.g.gn.n; ++i, ++nd) {
+        dims[nd] = op.g.gn.dim[i];
+        strd[nd] = op.g.gn.s1[i];
+      }
+      if (nd > 4) throw std::runtime_error("tensor-core output with more than 4 modes: " + op.tag);
+      for (int i = 0; i < 4; ++i) {
+        const int k = i - (4 - nd);
+        za.d[i] = k >= 0 ? (int)dims[k] : 1;
+        za.sC[i] = k >= 0 ? strd[k] : 0;
+      }
+      za.total = M * N;
+      za.cc = op.dtc == C64;
+      za.acc = 0;
+      za.nt = 0;
+      z.add_sc = op.sc;
+      z.add_oc = op.oc;
+      z.write = op.sc;
+      z.bytes = M * N * elem_bytes(op.dtc);
+      out.push_back(z);
+    }
+    out.push_back(t);
+  }
+  ops.swap(out);
 }
 
 }  // namespace tdcc

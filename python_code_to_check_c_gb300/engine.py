@@ -94,6 +94,11 @@ class CCEngine:
         check(self.lib.tdcc_set_precision(self.handle, m, int(slices)), "tdcc_set_precision")
         self.precision = mode
 
+    def check_errors(self):
+        """Synchronises and raises if a kernel recorded an error (an expired
+        bounded wait in a tensor-core kernel)."""
+        check(self.lib.tdcc_check_errors(self.handle), "tdcc_check_errors")
+
     def workspace_bytes(self) -> int:
         return int(self.lib.tdcc_workspace_bytes(self.handle))
 

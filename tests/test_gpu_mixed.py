@@ -1,0 +1,112 @@
+"""Mixed-precision form: contractions on the tensor cores as BF16 slice
+products (FP32 accumulate), everything else FP64.  Checked against the
+reference's golden residuals and against the FP64 GPU form.
+
+Tolerances (written here, met with S = 5 slices per operand):
+  residuals      relative 1e-9 (max |diff| / max |ref|)
+  mu_z(t)        |d mu| <= 1e-8 a.u. over the propagation vs the FP64 form
+"""
+import numpy as np
+import pytest
+
+from golden_util import CASES, load, rel_err
+
+pytestmark = pytest.mark.gpu
+
+RES_TOL = 1e-9
+MU_TOL = 1e-8
+
+
+def _np(x):
+    return x.detach().cpu().numpy()
+
+
+@pytest.fixture(scope="module", params=CASES[:2])
+def case(request):
+    from python_code_to_check_c_gb300.engine import CCEngine
+    d, sysm = load(request.param)
+    eng = CCEngine.from_system(sysm)
+    eng.set_precision("mixed", 5)
+    yield d, sysm, eng
+    eng.close()
+
+
+@pytest.mark.parametrize("name,fn,args", [
+    ("T1", "T1eq_rhs", "t"), ("T2", "T2eq_rhs", "t"),
+    ("L1", "lam_1eq_rhs", "l"), ("L2", "lam2eq_rhs", "l"),
+    ("T2_CC2", "T2eq_rhs_CC2", "t"), ("L1_CC2", "L1eq_rhs_CC2", "l"), ("L2_CC2", "L2eq_rhs_CC2", "l"),
+])
+def test_mixed_residual_close_to_reference(case, name, fn, args):
+    d, sysm, eng = case
+    a = (d["t1"], d["t2"]) if args == "t" else (d["t1"], d["t2"], d["l1"], d["l2"])
+    got = _np(getattr(eng, fn)(*a, d["F"]))
+    eng.check_errors()
+    err = rel_err(got, d[name])
+    assert err < RES_TOL, (name, err)
+
+
+def test_slices_control_the_error():
+    """More slices, smaller error (until FP64 round-off)."""
+    from python_code_to_check_c_gb300.engine import CCEngine
+    d, sysm = load("golden_o6_v10.npz")
+    eng = CCEngine.from_system(sysm)
+    errs = []
+    try:
+        for S in (3, 4, 5, 6):
+            eng.set_precision("mixed", S)
+            got = _np(eng.lam2eq_rhs(d["t1"], d["t2"], d["l1"], d["l2"], d["F"]))
+            eng.check_errors()
+            errs.append(rel_err(got, d["L2"]))
+    finally:
+        eng.close()
+    assert errs[0] > errs[2] and errs[1] > errs[2], errs
+    assert errs[3] < 1e-10, errs
+
+
+def test_mixed_large_contractions_use_tensor_cores():
+    from python_code_to_check_c_gb300._lib import make_field
+    from python_code_to_check_c_gb300.engine import CCEngine, profile_step
+    from python_code_to_check_c_gb300.system import synthetic_system
+    sysm = synthetic_system(10, 38, 144, seed=1038)
+    eng = CCEngine.from_system(sysm)
+    try:
+        eng.set_precision("mixed", 5)
+        o, v = sysm.o, sysm.v
+        rng = np.random.default_rng(3)
+        st = (0.01 * rng.standard_normal((o, v)) + 0j, 0.01 * rng.standard_normal((o, o, v, v)) + 0j,
+              0.01 * rng.standard_normal((o, v)) + 0j, 0.01 * rng.standard_normal((o, o, v, v)) + 0j)
+        recs = profile_step(eng, "CCSD", st, 0.0, 0.005, make_field("sin", 0.002, 0.923))
+        tc = [r for r in recs if r["backend"] == 1 and r["kind"] == 0]
+        f64 = [r for r in recs if r["backend"] == 0 and r["kind"] == 0]
+        assert tc, "no tensor-core contraction in the mixed step"
+        assert sum(r["flops"] for r in tc) > 20 * sum(r["flops"] for r in f64)
+        eng.check_errors()
+    finally:
+        eng.close()
+
+
+@pytest.mark.parametrize("method", ["CCSD", "CC2"])
+def test_mixed_trajectory_o10_v14(method):
+    """200 steps (dt 0.01, E = 0.002 sin(0.923 t)) from a converged ground state."""
+    from oracle.cc_oracle import CCOracle
+    from python_code_to_check_c_gb300._lib import make_field
+    from python_code_to_check_c_gb300.engine import CCEngine
+    from python_code_to_check_c_gb300.system import WORKLOADS, synthetic_system
+    sysm = synthetic_system(**WORKLOADS["ccsd_o10_v14"])
+    orc = CCOracle(sysm.tei(), sysm.o, mu=sysm.mu)
+    F = sysm.fock
+    t1 = np.zeros((sysm.o, sysm.v))
+    E, t1, t2 = orc.DIIS_solver(t1, orc.MP2_guess(F), F, 8, 40, 1e-15, method=method)
+    El, l1, l2 = orc.DIIS_solver_Lam(t1, t2, t1, t2, F, 8, 30, 1e-15, method=method)
+    gs = tuple(x + 0j for x in (t1, t2, l1, l2))
+    f = make_field("sin", 0.002, 0.923)
+    eng = CCEngine.from_system(sysm)
+    try:
+        _, mu64 = eng.propagate(method, gs, 0.0, 0.01, 200, f)
+        eng.set_precision("mixed", 5)
+        _, mumx = eng.propagate(method, gs, 0.0, 0.01, 200, f)
+        eng.check_errors()
+    finally:
+        eng.close()
+    err = np.abs(_np(mumx) - _np(mu64)).max()
+    assert err < MU_TOL, err
