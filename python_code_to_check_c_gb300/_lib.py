@@ -63,6 +63,7 @@ SIGNATURES = {
     "tdcc_set_precision": (_i, [_vp, _i, _i]),
     "tdcc_workspace_bytes": (_ll, [_vp]),
     "tdcc_check_errors": (_i, [_vp]),
+    "tdcc_set_tc_policy": (_i, [_vp, _ll, _i]),
     "tdcc_rhs": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tdcc_dipole": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "tdcc_rk4_step": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _i,

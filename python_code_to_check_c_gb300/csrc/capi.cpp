@@ -53,6 +53,8 @@ struct tdcc_system_s {
   int n_mu = 0;
   int prec_mode = TDCC_PREC_FP64;
   int slices = 5;
+  long long tc_min_macs = kTcMinMacs;  // tensor-core routing policy
+  int tc_min_k = 64;
   int device = 0;
   std::unique_ptr<ProgInst> rhs[2][4];
   std::unique_ptr<ProgInst> dens;
@@ -132,7 +134,7 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
     build_l1_cc2(p);
   else
     build_l2_cc2(p, p.ones("ones_v", s->dims.v));
-  p.select_backend(s->prec_mode, kTcMinMacs, s->slices);
+  p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
   pi->bases.assign(p.slots.size(), nullptr);
@@ -192,7 +194,9 @@ struct Prof {
   void add_prog(const std::vector<Program::Timed>& tm, int block, int stage) {
     for (const auto& t : tm) {
       const Op& op = *t.op;
-      const int kind = op.kind == OP_GEMM ? 0 : op.kind == OP_ADD ? 1 : 2;
+      const int kind = (op.kind == OP_GEMM || op.kind == OP_TCGEMM) ? 0
+                       : (op.kind == OP_ADD || op.kind == OP_PACK) ? 1
+                                                                   : 2;
       recs.push_back({op.tag, kind, block, stage, op.backend, (double)op.flops, (double)op.bytes, t.a, t.b});
     }
   }
@@ -292,6 +296,23 @@ int fail(int code, const std::string& m) {
   return code;
 }
 
+// drops the right-hand-side programs (and their workspace) and the captured
+// step graphs; they are rebuilt on next use
+void reset_programs(tdcc_system s) {
+  cudaDeviceSynchronize();
+  for (auto& mrow : s->rhs)
+    for (auto& pi : mrow)
+      if (pi) {
+        s->ws_bytes -= pi->bytes;
+        pi.reset();
+      }
+  for (auto& g : s->gexec)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
 bool valid_method(int m) { return m == TDCC_CCSD || m == TDCC_CC2; }
 
 }  // namespace
@@ -356,21 +377,19 @@ int tdcc_set_precision(tdcc_system s, int mode, int slices) {
   if (mode == TDCC_PREC_MIXED && (slices < 3 || slices > 7)) return fail(TDCC_ERR_ARG, "slices must be 3..7");
   if (mode == TDCC_PREC_FP64) slices = s->slices;
   if (mode == s->prec_mode && slices == s->slices) return TDCC_OK;
-  // programs are rebuilt (and their workspace reallocated) on next use
-  cudaDeviceSynchronize();
-  for (auto& mrow : s->rhs)
-    for (auto& pi : mrow)
-      if (pi) {
-        s->ws_bytes -= pi->bytes;
-        pi.reset();
-      }
-  for (auto& g : s->gexec)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  reset_programs(s);
   s->prec_mode = mode;
   s->slices = slices;
+  return TDCC_OK;
+}
+
+int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (min_macs < 0 || min_k < 1) return fail(TDCC_ERR_ARG, "min_macs >= 0 and min_k >= 1 required");
+  if (min_macs == s->tc_min_macs && min_k == s->tc_min_k) return TDCC_OK;
+  reset_programs(s);
+  s->tc_min_macs = min_macs;
+  s->tc_min_k = min_k;
   return TDCC_OK;
 }
 

@@ -465,7 +465,7 @@ cudaError_t Program::run(const std::vector<void*>& bases, cudaStream_t st, Phase
 
 static long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
 
-void Program::select_backend(int prec_mode, long long min_macs, int S) {
+void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k) {
   if (prec_mode != 1) return;
   if (S < 1 || S > 7) throw std::runtime_error("slices must be 1..7");
   constexpr int BM = 128, BN = 64, BK = 64;  // tensor-core tile (gemm_tc.h)
@@ -477,7 +477,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S) {
       continue;
     }
     const long long M = op.g.M, N = op.g.N, K = op.g.K;
-    if (M * N * K < min_macs || K < BK) {
+    if (M * N * K < min_macs || K < min_k) {
       out.push_back(op);
       continue;
     }

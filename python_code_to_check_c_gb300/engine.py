@@ -94,6 +94,10 @@ class CCEngine:
         check(self.lib.tdcc_set_precision(self.handle, m, int(slices)), "tdcc_set_precision")
         self.precision = mode
 
+    def set_tc_policy(self, min_macs: int = 1 << 21, min_k: int = 64):
+        """Which contractions the mixed mode sends to the tensor cores."""
+        check(self.lib.tdcc_set_tc_policy(self.handle, int(min_macs), int(min_k)), "tdcc_set_tc_policy")
+
     def check_errors(self):
         """Synchronises and raises if a kernel recorded an error (an expired
         bounded wait in a tensor-core kernel)."""
