@@ -39,7 +39,8 @@ struct ProgInst {
 
 // contractions with at least this many multiply-adds (and K >= 64) use the
 // tensor-core slice products in the mixed-precision mode
-constexpr long long kTcMinMacs = 1LL << 21;
+constexpr long long kTcMinMacs = 1LL << 18;
+constexpr int kTcMinK = 8;
 
 }  // namespace tdcc
 
@@ -54,7 +55,7 @@ struct tdcc_system_s {
   int prec_mode = TDCC_PREC_FP64;
   int slices = 5;
   long long tc_min_macs = kTcMinMacs;  // tensor-core routing policy
-  int tc_min_k = 64;
+  int tc_min_k = kTcMinK;
   int device = 0;
   std::unique_ptr<ProgInst> rhs[2][4];
   std::unique_ptr<ProgInst> dens;

@@ -55,44 +55,82 @@ __device__ __forceinline__ void decomp_tc(const ModeGroup& g, int l, long long& 
   }
 }
 
-__global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Row exponents are stored biased (e + kExpBias; 0 = all-zero row) so that
+// zero-initialised memory and atomicMax give the maximum directly.
+constexpr int kExpBias = 4096;
+__device__ __forceinline__ int row_exp(int biased) { return biased > 0 ? biased - kExpBias : 0; }
+
+// Pass 1: per packed row, the binary exponent e of max |x| (max = f 2^e,
+// f in [0.5, 1)).  One warp per (row, 256-wide K range), warp max, one
+// atomicMax per warp.
+__global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= p.rows_pad) return;
-  const int pr = warp;
-  const int m = p.cplx ? (pr >> 1) : pr;
-  const int part = p.cplx ? (pr & 1) : 0;
-  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
-  const size_t plane = (size_t)p.rows_pad * p.K_pad;
-  if (m >= p.rows) {
-    for (int k = lane; k < p.K_pad; k += 32)
-      for (int s = 0; s < p.S; ++s) out[s * plane + (size_t)pr * p.K_pad + k] = __float2bfloat16_rn(0.f);
-    if (lane == 0) p.exps[pr] = 0;
-    return;
-  }
+  const int kr = (p.K + 255) / 256;
+  if (warp >= (long long)p.rows * kr) return;
+  const int m = (int)(warp / kr), k0 = (int)(warp % kr) * 256;
   long long roff;
   decomp_tc(p.gr, m, roff);
   const double* src = static_cast<const double*>(p.src);
-  auto load = [&](int k) -> double {
-    long long ko;
-    decomp_tc(p.gk, k, ko);
-    const long long e = roff + ko;
-    return p.cplx ? src[2 * e + part] : src[e];
-  };
-  double mx = 0.0;
-  for (int k = lane; k < p.K; k += 32) mx = fmax(mx, fabs(load(k)));
-  for (int d = 16; d > 0; d >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, d));
-  int e = 0;
-  if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
-  for (int k = lane; k < p.K_pad; k += 32) {
-    double r = k < p.K ? ldexp(load(k), -e) : 0.0;
+  double mre = 0.0, mim = 0.0;
+#pragma unroll 4
+  for (int j = 0; j < 8; ++j) {
+    const int k = k0 + lane + 32 * j;
+    if (k < p.K) {
+      long long ko;
+      decomp_tc(p.gk, k, ko);
+      const long long e = roff + ko;
+      if (p.cplx) {
+        mre = fmax(mre, fabs(src[2 * e]));
+        mim = fmax(mim, fabs(src[2 * e + 1]));
+      } else {
+        mre = fmax(mre, fabs(src[e]));
+      }
+    }
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    mre = fmax(mre, __shfl_xor_sync(0xffffffffu, mre, d));
+    mim = fmax(mim, __shfl_xor_sync(0xffffffffu, mim, d));
+  }
+  if (lane == 0) {
+    int e;
+    if (mre > 0.0) {
+      frexp(mre, &e);
+      atomicMax(&p.exps[p.cplx ? 2 * m : m], e + kExpBias);
+    }
+    if (p.cplx && mim > 0.0) {
+      frexp(mim, &e);
+      atomicMax(&p.exps[2 * m + 1], e + kExpBias);
+    }
+  }
+}
+
+// Pass 2: one thread per packed (row, k), K fastest: scale by 2^-e and cut
+// into S slices of 7 bits; zero in the padding.
+__global__ void __launch_bounds__(256) pack_slice_kernel(const PackArgs p) {
+  const long long total = (long long)p.rows_pad * p.K_pad;
+  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+  const double* src = static_cast<const double*>(p.src);
+  const size_t plane = (size_t)total;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int pr = (int)(idx / p.K_pad), k = (int)(idx % p.K_pad);
+    const int m = p.cplx ? (pr >> 1) : pr;
+    double r = 0.0;
+    if (m < p.rows && k < p.K) {
+      long long ro, ko;
+      decomp_tc(p.gr, m, ro);
+      decomp_tc(p.gk, k, ko);
+      const long long e = ro + ko;
+      const double x = p.cplx ? src[2 * e + (pr & 1)] : src[e];
+      r = ldexp(x, -row_exp(p.exps[pr]));
+    }
     for (int s = 0; s < p.S; ++s) {
       const double q = rint(ldexp(r, 7 * (s + 1)));
       r -= ldexp(q, -7 * (s + 1));
-      out[s * plane + (size_t)pr * p.K_pad + k] = __float2bfloat16_rn((float)q);
+      out[s * plane + idx] = __float2bfloat16_rn((float)q);
     }
   }
-  if (lane == 0) p.exps[pr] = e;
 }
 
 // ---------------------------------------------------------------------------
@@ -331,11 +369,11 @@ __global__ void __launch_bounds__(192, 1)
     if (!__any_sync(0xffffffffu, sh->abort != 0)) {
       // scale back and write
       const int prow = mt * TC_BM + row;          // packed row of A
-      const int ea = prow < g.rowsA_pad ? g.expA[prow] : 0;
+      const int ea = prow < g.rowsA_pad ? row_exp(g.expA[prow]) : 0;
 #pragma unroll
       for (int j = 0; j < TC_BN; ++j) {
         const int pcol = nt * TC_BN + j;
-        const int eb = g.expB[pcol];
+        const int eb = row_exp(g.expB[pcol]);
         acc[j] = ldexp(acc[j], ea + eb);
       }
       const int m = AC ? (prow >> 1) : prow;
@@ -443,8 +481,17 @@ static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, i
 }
 
 cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
-  const long long threads = (long long)p.rows_pad * 32;
-  pack_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(p);
+  cudaError_t e = cudaMemsetAsync(p.exps, 0, (size_t)p.rows_pad * sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const long long warps = (long long)p.rows * ((p.K + 255) / 256);
+  if (warps > 0) {
+    pack_rowmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(p);
+    count_launch();
+  }
+  const long long total = (long long)p.rows_pad * p.K_pad;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  pack_slice_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
   count_launch();
   return cudaGetLastError();
 }
