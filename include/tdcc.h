@@ -98,12 +98,12 @@ int tdcc_system_create(int o, int v, const double* tei, const double* fock,
 int tdcc_system_destroy(tdcc_system s);
 
 /* Selects the contraction arithmetic (TDCC_PREC_*) and, for the mixed mode,
-   the number of BF16 slices per operand (3..7).                           */
+   the number of BF16 slices per operand (2..6; 7 bits each).             */
 int tdcc_set_precision(tdcc_system s, int mode, int slices);
 
 /* Mixed mode routing: contractions with at least min_macs multiply-adds and
    a contracted extent K >= min_k run on the tensor cores (defaults 2^18 and
-   8); the rest stay FP64.  (0, 1) sends every contraction to the tensor
+   32); the rest stay FP64.  (0, 1) sends every contraction to the tensor
    cores, which tests use at small sizes.                                  */
 int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k);
 

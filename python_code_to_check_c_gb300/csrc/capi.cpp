@@ -40,7 +40,7 @@ struct ProgInst {
 // contractions with at least this many multiply-adds (and K >= 64) use the
 // tensor-core slice products in the mixed-precision mode
 constexpr long long kTcMinMacs = 1LL << 18;
-constexpr int kTcMinK = 8;
+constexpr int kTcMinK = 32;
 
 }  // namespace tdcc
 
@@ -375,7 +375,7 @@ int tdcc_set_precision(tdcc_system s, int mode, int slices) {
   if (mode != TDCC_PREC_FP64 && mode != TDCC_PREC_MIXED) return fail(TDCC_ERR_ARG, "bad precision mode");
   if (mode == TDCC_PREC_MIXED && !tc_available())
     return fail(TDCC_ERR_STATE, "tensor-core backend not built into this library");
-  if (mode == TDCC_PREC_MIXED && (slices < 3 || slices > 7)) return fail(TDCC_ERR_ARG, "slices must be 3..7");
+  if (mode == TDCC_PREC_MIXED && (slices < 2 || slices > 6)) return fail(TDCC_ERR_ARG, "slices must be 2..6");
   if (mode == TDCC_PREC_FP64) slices = s->slices;
   if (mode == s->prec_mode && slices == s->slices) return TDCC_OK;
   reset_programs(s);

@@ -105,30 +105,48 @@ __global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
   }
 }
 
-// Pass 2: one thread per packed (row, k), K fastest: scale by 2^-e and cut
-// into S slices of 7 bits; zero in the padding.
+// floor(|x| 2^(nbits - e)) as an integer, from the bits of x (exact; no FP64
+// arithmetic).  Requires |x| < 2^e and nbits <= 56, so the result < 2^nbits.
+__device__ __forceinline__ unsigned long long fixed_point(double x, int e, int nbits) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+  const int E = (int)(u >> 52);
+  if (E == 0) return 0ull;  // zero or subnormal: below every slice
+  const unsigned long long M = (u & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  const int sh = E - 1075 - e + nbits;  // |x| = M 2^(E-1075)
+  if (sh >= 0) return M << sh;
+  if (sh <= -64) return 0ull;
+  return M >> (-sh);
+}
+
+// Pass 2: one block per packed row, threads over K: |x| 2^-e truncated to
+// 7S bits and cut into S signed 7-bit digits (|q_s| <= 127, exact in BF16):
+//   x 2^-e ~= sum_s q_s 2^(-7s).   Zero in the padding.
 __global__ void __launch_bounds__(256) pack_slice_kernel(const PackArgs p) {
-  const long long total = (long long)p.rows_pad * p.K_pad;
+  const int pr = blockIdx.x;
+  const int m = p.cplx ? (pr >> 1) : pr;
   __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
   const double* src = static_cast<const double*>(p.src);
-  const size_t plane = (size_t)total;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int pr = (int)(idx / p.K_pad), k = (int)(idx % p.K_pad);
-    const int m = p.cplx ? (pr >> 1) : pr;
-    double r = 0.0;
-    if (m < p.rows && k < p.K) {
-      long long ro, ko;
-      decomp_tc(p.gr, m, ro);
+  const size_t plane = (size_t)p.rows_pad * p.K_pad;
+  const size_t rowbase = (size_t)pr * p.K_pad;
+  const bool live = m < p.rows;
+  long long ro = 0;
+  if (live) decomp_tc(p.gr, m, ro);
+  const int e = row_exp(p.exps[pr]);
+  const int nbits = 7 * p.S;
+  for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < p.K_pad; k += gridDim.y * blockDim.x) {
+    unsigned long long f = 0ull;
+    bool neg = false;
+    if (live && k < p.K) {
+      long long ko;
       decomp_tc(p.gk, k, ko);
-      const long long e = ro + ko;
-      const double x = p.cplx ? src[2 * e + (pr & 1)] : src[e];
-      r = ldexp(x, -row_exp(p.exps[pr]));
+      const long long el = ro + ko;
+      const double x = p.cplx ? src[2 * el + (pr & 1)] : src[el];
+      f = fixed_point(x, e, nbits);
+      neg = x < 0.0;
     }
     for (int s = 0; s < p.S; ++s) {
-      const double q = rint(ldexp(r, 7 * (s + 1)));
-      r -= ldexp(q, -7 * (s + 1));
-      out[s * plane + idx] = __float2bfloat16_rn((float)q);
+      const int q = (int)((f >> (7 * (p.S - 1 - s))) & 127ull);
+      out[s * plane + rowbase + k] = __float2bfloat16_rn((float)(neg ? -q : q));
     }
   }
 }
@@ -353,15 +371,23 @@ __global__ void __launch_bounds__(192, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      for (int L = 2; L <= S + 1; ++L) {
-        const double w = ldexp(1.0, -7 * L);
+      // The level sums are integers (products of integer slices); combine
+      // them exactly in 64-bit integers, sum_L v_L 2^(7(S+1-L)) < 2^(24+7(S-1)),
+      // and convert once per chunk (exact for S <= 5).
 #pragma unroll
-        for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+      for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+        long long comb[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) comb[j] = 0;
+        for (int L = 2; L <= S + 1; ++L) {
           float v[16];
           tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((L - 2) * TC_BN + j0), v);
+          const int sh = 7 * (S + 1 - L);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) acc[j0 + j] = fma((double)v[j], w, acc[j0 + j]);
+          for (int j = 0; j < 16; ++j) comb[j] += __float2ll_rn(v[j]) * (1LL << sh);
         }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[j0 + j] += (double)comb[j];
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(smem_u32(&sh->accempty));
@@ -374,7 +400,7 @@ __global__ void __launch_bounds__(192, 1)
       for (int j = 0; j < TC_BN; ++j) {
         const int pcol = nt * TC_BN + j;
         const int eb = row_exp(g.expB[pcol]);
-        acc[j] = ldexp(acc[j], ea + eb);
+        acc[j] = ldexp(acc[j], ea + eb - 7 * (S + 1));
       }
       const int m = AC ? (prow >> 1) : prow;
       const bool odd = AC && (lane & 1);
@@ -488,10 +514,9 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
     pack_rowmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(p);
     count_launch();
   }
-  const long long total = (long long)p.rows_pad * p.K_pad;
-  long long blocks = (total + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
-  pack_slice_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
+  const int threads = p.K_pad >= 256 ? 256 : p.K_pad;
+  const int by = (p.K_pad + threads - 1) / threads > 8 ? 8 : (p.K_pad + threads - 1) / threads;
+  pack_slice_kernel<<<dim3(p.rows_pad, by), threads, 0, st>>>(p);
   count_launch();
   return cudaGetLastError();
 }

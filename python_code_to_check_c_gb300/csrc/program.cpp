@@ -576,12 +576,22 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     a.ar = op.g.ar;
     a.ai = op.g.ai;
     a.acc = op.g.acc;
-    // split K so that few output tiles still occupy the SMs
+    // split K so that few output tiles still occupy the SMs: one CTA per SM,
+    // cost = waves x (K blocks per CTA + fixed pipeline/epilogue overhead)
     const long long ctas = (rB / BN) * (rA / BM);
     long long splits = 1;
-    if (ctas < 152 && a.kblocks >= 4) {
-      splits = std::min<long long>((152 + ctas - 1) / ctas, a.kblocks / 2);
-      splits = std::max<long long>(splits, 1);
+    {
+      double best = 1e300;
+      const long long maxs = std::max<long long>(1, std::min<long long>(a.kblocks, 64));
+      for (long long sp = 1; sp <= maxs; ++sp) {
+        const long long waves = (ctas * sp + 151) / 152;
+        const long long per = (a.kblocks + sp - 1) / sp;
+        const double cost = (double)waves * (double)(per * S + 6);
+        if (cost < best - 1e-9) {
+          best = cost;
+          splits = sp;
+        }
+      }
     }
     a.kb_per_split = (int)((a.kblocks + splits - 1) / splits);
     splits = (a.kblocks + a.kb_per_split - 1) / a.kb_per_split;

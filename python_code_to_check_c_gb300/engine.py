@@ -94,7 +94,7 @@ class CCEngine:
         check(self.lib.tdcc_set_precision(self.handle, m, int(slices)), "tdcc_set_precision")
         self.precision = mode
 
-    def set_tc_policy(self, min_macs: int = 1 << 18, min_k: int = 8):
+    def set_tc_policy(self, min_macs: int = 1 << 18, min_k: int = 32):
         """Which contractions the mixed mode sends to the tensor cores."""
         check(self.lib.tdcc_set_tc_policy(self.handle, int(min_macs), int(min_k)), "tdcc_set_tc_policy")
 
