@@ -32,6 +32,14 @@ struct ProgInst {
   std::vector<void*> bases;
   std::vector<void*> owned;  // this program's workspace allocations
   long long bytes = 0;
+  bool setup_done = false;   // integral-only ops (e.g. packed integral blocks) ran
+  // runs the integral-only ops once, eagerly, on `st`
+  cudaError_t setup(cudaStream_t st) {
+    if (setup_done) return cudaSuccess;
+    const cudaError_t e = prog->run(bases, st, Program::SETUP);
+    if (e == cudaSuccess) setup_done = true;
+    return e;
+  }
   ~ProgInst() {
     for (void* p : owned) cudaFree(p);
   }
@@ -230,6 +238,7 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
   const long long nn = (long long)s->dims.n * s->dims.n;
   std::vector<Program::Timed> tm;
   B[S_F] = s->Fs;
+  CK(pi.setup(st));
   CK(p.run(B, st, Program::PROLOGUE, pf ? &tm : nullptr));
   if (pf) pf->add_prog(tm, b, 0);
   for (int stage = 1; stage <= 4; ++stage) {
@@ -434,7 +443,8 @@ int tdcc_rhs(tdcc_system s, int method, int block, const void* t1, const void* t
     B[S_L2] = const_cast<void*>(l2);
     B[S_F] = const_cast<void*>(F);
     B[S_OUT] = out;
-    cudaError_t e = pi.prog->run(B, static_cast<cudaStream_t>(stream), Program::ALL);
+    cudaError_t e = pi.setup(static_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess) e = pi.prog->run(B, static_cast<cudaStream_t>(stream), Program::DYNAMIC);
     if (e != cudaSuccess) return TDCC_ERR_CUDA;
   } catch (const std::exception& ex) {
     return fail(TDCC_ERR_CUDA, ex.what());
@@ -519,7 +529,8 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
           g = nullptr;
         }
       // build programs (allocations) before capture
-      for (int b = 0; b < 4; ++b) get_rhs(s, method, b);
+      for (int b = 0; b < 4; ++b) CK(get_rhs(s, method, b).setup(s->main));
+      CK(cudaStreamSynchronize(s->main));
       get_density(s);
       const long long before_capture = launch_count();
       for (int k = 0; k < 2; ++k) {
@@ -685,7 +696,8 @@ std::string program_json(const Program& p) {
   for (size_t i = 0; i < p.ops.size(); ++i) {
     const Op& op = p.ops[i];
     j += i ? "," : "";
-    const std::string var = op.varying ? "true" : "false";
+    const std::string var =
+        std::string(op.varying ? "true" : "false") + ",\"const\":" + (op.is_const ? "true" : "false");
     if (op.kind == OP_GEMM) {
       const GemmArgs& g = op.g;
       j += "{\"kind\":\"gemm\",\"tag\":\"" + op.tag + "\",\"varying\":" + var +

@@ -173,6 +173,7 @@ struct Op {
   std::vector<int> reads;
   int write = -1;
   bool varying = true;
+  bool is_const = false;   // depends on the integrals only: run once per system
 };
 
 struct SlotInfo {
@@ -236,7 +237,11 @@ class Program {
   // device allocation of workspace slots (returns bytes allocated)
   long long allocate(std::vector<void*>& bases, std::vector<void*>& owned);
 
-  enum Phase { ALL = 0, PROLOGUE = 1, STAGE = 2 };
+  // ALL: every op.  SETUP: ops that depend on the integrals only (once per
+  // system).  PROLOGUE: the rest of the ops independent of the varying
+  // slots (once per RK4 step).  STAGE: ops on the varying slots.  DYNAMIC:
+  // every op except SETUP ones.
+  enum Phase { ALL = 0, PROLOGUE = 1, STAGE = 2, SETUP = 3, DYNAMIC = 4 };
   // `timed`, when given, receives (op, start event, stop event) per launch;
   // the caller synchronises and destroys the events.
   struct Timed {

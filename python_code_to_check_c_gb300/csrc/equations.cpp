@@ -55,19 +55,35 @@ View make_fme(P& p, const View& xg) {
 // (term1, the Wmnij_2/Wabef_2 tau ladders, the t1 t1 ring, term7, term8;
 // CCSD_Helper.py:284-306) into C2.
 struct T2Const {
-  View C2, tau1, tt, wabef2;
+  View C2, tau1, tt;
 };
+
+// Particle-particle ladder with a Wabef built from the integrals and t1,
+//   c * sum_ef Wx_abef X_ijef,
+//   Wx = <ab||ef> + P(ab)[-<am||ef> t1_mb] + w <mn||ef> tau1_mnab,
+// without forming the v^4 tensor Wx (same algebra, re-associated):
+//   c <ab||ef> X_ijef  -  c P(ab) sum_m t1_mb U_ijam  +  c w sum_mn tau1_mnab Z_mnij
+// with U_ijam = <am||ef> X_ijef (o^3 v^3) and Z_mnij = <mn||ef> X_ijef (o^4 v^2).
+// The vvvv ladder runs on the integrals themselves, whose packed operand is
+// a per-system constant.  Z is returned for reuse (Wmnij).
+View ladder(P& p, const View& t1, const View& tau1, const View& X, double c, double w,
+            const View& out, const char* tag) {
+  p.ein("abef,ijef->ijab", c, p.G("vvvv"), X, out, true);
+  View u = p.ws(std::string(tag) + "_U", "oovo");  // [i,j,a,m]
+  p.ein("amef,ijef->ijam", 1.0, p.G("vovv"), X, u, false);
+  View y = p.ws(std::string(tag) + "_Ut1", "oovv");
+  p.ein("ijam,mb->ijab", -1.0, u, t1, y, false);
+  p.acc_pab(out, y, c);
+  View z = p.ws(std::string(tag) + "_Z", "oooo");
+  p.ein("mnef,ijef->mnij", 1.0, p.G("oovv"), X, z, false);
+  p.ein("mnij,mnab->ijab", c * w, z, tau1, out, true);
+  return z;
+}
 
 T2Const build_t2_const(P& p, const View& t1) {
   T2Const r;
   r.tt = make_tt(p, t1, "tt");
   r.tau1 = make_tau1(p, t1, "tau1");
-  // Wabef_2 = <ab||ef> + P(ab)[-<am||ef> t1_mb] + 1/4 <mn||ef> tau1_mnab
-  r.wabef2 = p.ws("Wabef_2", "vvvv");
-  View x = p.ws("Wabef_2_x", "vvvv");
-  p.ein("amef,mb->abef", -1.0, p.G("vovv"), t1, x, false);
-  p.add(r.wabef2, false, {T(1.0, p.G("vvvv")), T(1.0, x), T(-1.0, x.swap(0, 1))});
-  p.ein("mnef,mnab->abef", 0.25, p.G("oovv"), r.tau1, r.wabef2, true);
   // Wmnij_2 = <mn||ij> + P(ij)[<mn||ie> t1_je] + P(ij)[1/4 <mn||ef> tt_ijef]
   View wmnij2 = p.ws("Wmnij_2", "oooo");
   View y = p.ws("Wmnij_2_y", "oooo");
@@ -75,10 +91,12 @@ T2Const build_t2_const(P& p, const View& t1) {
   p.ein("mnef,ijef->mnij", 0.25, p.G("oovv"), r.tt, y, true);
   p.add(wmnij2, false, {T(1.0, p.G("oooo")), T(1.0, y), T(-1.0, y.swap(2, 3))});
   // C2 = <ij||ab> + 1/2 Wmnij_2 tau1 + 1/2 Wabef_2 tau1 + ...
+  // (Wabef_2 = <ab||ef> + P(ab)[-<am||ef> t1_mb] + 1/4 <mn||ef> tau1_mnab,
+  //  CCSD_Helper.py:240-252, applied through `ladder`)
   r.C2 = p.ws("C2", "oovv");
   p.copy(r.C2, p.G("oovv"));
   p.ein("mnij,mnab->ijab", 0.5, wmnij2, r.tau1, r.C2, true);
-  p.ein("abef,ijef->ijab", 0.5, r.wabef2, r.tau1, r.C2, true);
+  ladder(p, t1, r.tau1, r.tau1, 0.5, 0.25, r.C2, "L2t1");
   // ring with t1 t1: -P(ij)P(ab) sum_me <mb||ej> t1_ie t1_ma
   View rt = p.ws("ring_t1_a", "ovoo");  // [m,b,i,j]
   p.ein("mbej,ie->mbij", 1.0, p.G("ovvo"), t1, rt, false);
@@ -139,12 +157,6 @@ void build_t2_ccsd(P& p) {
   const View t1 = p.amp(S_T1), t2 = p.amp(S_T2), out = p.out(4);
   T2Const k = build_t2_const(p, t1);
   View xg = make_xg(p, t1);
-  // Wabef without its t2 term (CCSD_Helper.py:227-238):
-  //   Wc = <ab||ef> + P(ab)[-<am||ef> t1_mb] + P(ab)[1/2 <mn||ef> t1_ma t1_nb]
-  //      = Wabef_2 + 1/4 <mn||ef> tau1_mnab
-  View wc = p.ws("Wabef_c", "vvvv");
-  p.copy(wc, k.wabef2);
-  p.ein("mnef,mnab->abef", 0.25, p.G("oovv"), k.tau1, wc, true);
   // Wmnij without its t2 term (CCSD_Helper.py:199-210):
   //   Wmnij_c = <mn||ij> + P(ij)[<mn||ie> t1_je] + 1/2 <mn||ef> tau1_ijef
   View wmn_c = p.ws("Wmnij_c", "oooo");
@@ -186,13 +198,6 @@ void build_t2_ccsd(P& p) {
   p.ein("me,je->mj", 0.5, fme, t1, fmi, true);
   View x3 = p.ws("t2_term3", "oovv");
   p.ein("mj,imab->ijab", -1.0, fmi, t2, x3, false);
-  // term44 + the t2 t2 half of term55.  With Z_mnij = sum_ef <mn||ef> t2_ijef:
-  //   Wmnij = Wmnij_c + Z/4 and  1/2 sum_ef (1/4 <mn||ef> t2_mnab) t2_ijef
-  //   = 1/8 sum_mn Z_mnij t2_mnab, so  term44 + that = 1/2 (Wmnij_c + Z/2) t2.
-  View z = p.ws("Z", "oooo");
-  p.ein("mnef,ijef->mnij", 1.0, p.G("oovv"), t2, z, false);
-  View wtot = p.ws("Wmnij_tot", "oooo");
-  p.add(wtot, false, {T(1.0, wmn_c), T(0.5, z)});
   // ring: Wmbej = Wmbej_c - 1/2 <mn||ef> t2_jnfb ; P(ij)P(ab) Wmbej t2_imae
   View wmbej = p.ws("Wmbej", "ovvo");
   p.copy(wmbej, wmbej_c);
@@ -203,8 +208,16 @@ void build_t2_ccsd(P& p) {
   p.copy(out, k.C2);
   p.acc_pab(out, x2);
   p.acc_pij(out, x3);
+  // particle-particle ladder 1/2 Wabef t2 (CCSD_Helper.py:227-238, 294) with
+  //   Wabef = <ab||ef> + P(ab)[-<am||ef> t1_mb] + 1/2 <mn||ef> tau1_mnab
+  //           + 1/4 <mn||ef> t2_mnab;
+  // the last piece gives 1/8 sum_mn Z_mnij t2_mnab, Z_mnij = <mn||ef> t2_ijef,
+  // which joins term44: 1/2 Wmnij t2 with Wmnij = Wmnij_c + Z/4, so
+  //   term44 + that = 1/2 (Wmnij_c + Z/2) t2.
+  View z = ladder(p, t1, k.tau1, t2, 0.5, 0.5, out, "L2t2");
+  View wtot = p.ws("Wmnij_tot", "oooo");
+  p.add(wtot, false, {T(1.0, wmn_c), T(0.5, z)});
   p.ein("mnij,mnab->ijab", 0.5, wtot, t2, out, true);
-  p.ein("abef,ijef->ijab", 0.5, wc, t2, out, true);  // particle-particle ladder
   p.acc_pijab(out, ring);
 }
 
@@ -229,10 +242,12 @@ void build_t2_cc2(P& p) {
 // ---------------------------------------------------------------------------
 namespace {
 struct LamConst {
-  View xg, tt, fea_c, fim_c, wieam, wmnij, wabef, wfiea, wmina;
+  View xg, tt, tauq, fea_c, fim_c, wieam, wmnij, wfiea, wmina;
 };
 
-LamConst build_lam_const(P& p, const View& t1, const View& t2, bool need_vvvv) {
+// LSWabef (CCSD_Helper.py:598-607) is never formed: its two uses are
+// re-associated where they occur (lsw_ladder, and term3 of LRWefam).
+LamConst build_lam_const(P& p, const View& t1, const View& t2) {
   LamConst r;
   r.xg = make_xg(p, t1);
   r.tt = make_tt(p, t1, "tt");
@@ -255,21 +270,14 @@ LamConst build_lam_const(P& p, const View& t1, const View& t2, bool need_vvvv) {
   p.ein("eifa,mf->ieam", 1.0, p.G("vovv"), t1, r.wieam, true);
   p.ein("nima,ne->ieam", -1.0, p.G("ooov"), t1, r.wieam, true);
   p.ein("ijab,mjbe->ieam", -1.0, p.G("oovv"), tau_f, r.wieam, true);
-  // tau_q = 1/4 t2 + 1/2 tt  (LSWmnij, LSWabef)
-  View tauq = p.ws("tau_q", "oovv");
-  p.add(tauq, false, {T(0.25, t2), T(0.5, r.tt)});
+  // tau_q = 1/4 t2 + 1/2 tt  (LSWmnij, LSWabef, LRWefam, LRWibjm)
+  r.tauq = p.ws("tau_q", "oovv");
+  p.add(r.tauq, false, {T(0.25, t2), T(0.5, r.tt)});
   // LSWmnij (CCSD_Helper.py:586-595)
   r.wmnij = p.ws("LSWmnij", "oooo");
   p.copy(r.wmnij, p.G("oooo"), 0.5);
   p.ein("ijme,ne->ijmn", 1.0, p.G("ooov"), t1, r.wmnij, true);
-  p.ein("ijfe,mnfe->ijmn", 1.0, p.G("oovv"), tauq, r.wmnij, true);
-  // LSWabef (CCSD_Helper.py:598-607)
-  if (need_vvvv) {
-    r.wabef = p.ws("LSWabef", "vvvv");
-    p.copy(r.wabef, p.G("vvvv"), 0.5);
-    p.ein("emab,mf->efab", -1.0, p.G("vovv"), t1, r.wabef, true);
-    p.ein("nmab,nmef->efab", 1.0, p.G("oovv"), tauq, r.wabef, true);
-  }
+  p.ein("ijfe,mnfe->ijmn", 1.0, p.G("oovv"), r.tauq, r.wmnij, true);
   // LWfiea, LWmina (CCSD_Helper.py:533-550)
   r.wfiea = p.ws("LWfiea", "vovv");
   p.copy(r.wfiea, p.G("vovv"));
@@ -301,13 +309,22 @@ View make_lrfim(P& p, const View& t1, const View& fim_c) {
 void build_l1_ccsd(P& p) {
   const View t1 = p.amp(S_T1), t2 = p.amp(S_T2), l1 = p.amp(S_L1), l2 = p.amp(S_L2);
   const View out = p.out(2);
-  LamConst k = build_lam_const(p, t1, t2, true);
-  View tauq = p.ws("tau_q1", "oovv");
-  p.add(tauq, false, {T(0.25, t2), T(0.5, k.tt)});
+  LamConst k = build_lam_const(p, t1, t2);
+  const View tauq = k.tauq;
   // LRWefam without its Fme term (CCSD_Helper.py:488-505)
   View wefam = p.ws("LRWefam_c", "vvvo");
   p.copy(wefam, p.G("vvvo"), 0.5);
-  p.ein("efab,mb->efam", 1.0, k.wabef, t1, wefam, true);
+  // term3  sum_b LSWabef_efab t1_mb  with LSWabef = 1/2 <ef||ab>
+  //   - <em||ab> t1_mf + <nm||ab> tau_q_nmef  (CCSD_Helper.py:598-607), re-associated:
+  //   1/2 <ef||ab> t1_mb  -  sum_x t1_xf Q_exam  +  sum_nk tau_q_nkef R_nkam,
+  //   Q_exam = <ex||ab> t1_mb,  R_nkam = <nk||ab> t1_mb
+  p.ein("efab,mb->efam", 0.5, p.G("vvvv"), t1, wefam, true);
+  View q3 = p.ws("LRWefam_Q", "vovo");
+  p.ein("exab,mb->exam", 1.0, p.G("vovv"), t1, q3, false);
+  p.ein("exam,xf->efam", -1.0, q3, t1, wefam, true);
+  View r3 = p.ws("LRWefam_R", "oovo");
+  p.ein("nkab,mb->nkam", 1.0, p.G("oovv"), t1, r3, false);
+  p.ein("nkef,nkam->efam", 1.0, tauq, r3, wefam, true);
   View jfam = p.ws("LRWefam_jfam", "ovvo");
   p.copy(jfam, p.G("ovvo"), -1.0);
   p.ein("jnab,nmfb->jfam", 1.0, p.G("oovv"), t2, jfam, true);
@@ -364,7 +381,7 @@ void build_l1_ccsd(P& p) {
 void build_l2_ccsd(P& p) {
   const View t1 = p.amp(S_T1), t2 = p.amp(S_T2), l1 = p.amp(S_L1), l2 = p.amp(S_L2);
   const View out = p.out(4);
-  LamConst k = build_lam_const(p, t1, t2, true);
+  LamConst k = build_lam_const(p, t1, t2);
   // l2-independent part: <ij||ab> + P(ij) Wejab l1 - P(ab) Wijmb l1
   //   + P(ij)P(ab) Xg_jb l1_ia  (the t1 part of Fme (x) l1)
   View cl2 = p.ws("L2_c", "oovv");
@@ -400,7 +417,18 @@ void build_l2_ccsd(P& p) {
   p.acc_pab(out, x2);
   p.acc_pij(out, x3);
   p.ein("ijmn,mnab->ijab", 1.0, k.wmnij, l2, out, true);
-  p.ein("efab,ijef->ijab", 1.0, k.wabef, l2, out, true);  // particle-particle ladder
+  // particle-particle ladder sum_ef LSWabef_efab l2_ijef (term5) with
+  //   LSWabef = 1/2 <ef||ab> - <em||ab> t1_mf + <nm||ab> tau_q_nmef,
+  // re-associated so the v^4 tensor is never formed:
+  //   1/2 <ef||ab> l2_ijef - <em||ab> Y_ijem + <nm||ab> Zq_nmij,
+  //   Y_ijem = t1_mf l2_ijef,  Zq_nmij = tau_q_nmef l2_ijef
+  p.ein("efab,ijef->ijab", 0.5, p.G("vvvv"), l2, out, true);
+  View yl = p.ws("l2_Y", "oovo");
+  p.ein("mf,ijef->ijem", 1.0, t1, l2, yl, false);
+  p.ein("emab,ijem->ijab", -1.0, p.G("vovv"), yl, out, true);
+  View zq = p.ws("l2_Zq", "oooo");
+  p.ein("nmef,ijef->nmij", 1.0, k.tauq, l2, zq, false);
+  p.ein("nmab,nmij->ijab", 1.0, p.G("oovv"), zq, out, true);
   p.acc_pijab(out, x89);
 }
 

@@ -377,6 +377,31 @@ void Program::analyse(const std::vector<int>& varying_slots) {
       }
     }
   }
+  // constant ops: (transitively) independent of every caller-bound slot
+  // except the integrals, and writing slots no other op writes
+  std::vector<char> dyn(slots.size(), 0);
+  for (int s : {S_F, S_T1, S_T2, S_L1, S_L2, S_OUT, S_MU, S_RES}) dyn[s] = 1;
+  std::vector<char> opdyn(ops.size(), 0);
+  changed = true;
+  while (changed) {
+    changed = false;
+    for (size_t i = 0; i < ops.size(); ++i) {
+      const Op& op = ops[i];
+      bool d = opdyn[i] || op.kind == OP_TRACE;
+      for (int r : op.reads)
+        if (r >= 0 && dyn[r]) d = true;
+      if (op.write >= 0 && dyn[op.write]) d = true;
+      if (d && !opdyn[i]) {
+        opdyn[i] = 1;
+        changed = true;
+      }
+      if (d && op.write >= 0 && !dyn[op.write]) {
+        dyn[op.write] = 1;
+        changed = true;
+      }
+    }
+  }
+  for (size_t i = 0; i < ops.size(); ++i) ops[i].is_const = !opdyn[i];
 }
 
 long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned) {
@@ -408,7 +433,9 @@ static inline const void* at(const std::vector<void*>& b, int slot, long long of
 cudaError_t Program::run(const std::vector<void*>& bases, cudaStream_t st, Phase ph,
                          std::vector<Timed>* timed) const {
   for (const auto& op : ops) {
-    if (ph == PROLOGUE && op.varying) continue;
+    if (ph == SETUP && !op.is_const) continue;
+    if (ph == DYNAMIC && op.is_const) continue;
+    if (ph == PROLOGUE && (op.varying || op.is_const)) continue;
     if (ph == STAGE && !op.varying) continue;
     cudaError_t e = cudaSuccess;
     Timed tm{&op, nullptr, nullptr};

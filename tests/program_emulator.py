@@ -36,7 +36,9 @@ class Emulator:
 
     def run(self, phase="all"):
         for op in self.p["ops"]:
-            if phase == "prologue" and op["varying"]:
+            if phase == "setup" and not op.get("const"):
+                continue
+            if phase == "prologue" and (op["varying"] or op.get("const")):
                 continue
             if phase == "stage" and not op["varying"]:
                 continue

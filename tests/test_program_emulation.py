@@ -56,6 +56,7 @@ def test_prologue_independent_of_varying_inputs(case, method, block):
     good_f = e.bufs[S_F].copy()
     e.bufs[vslot] = np.full_like(good_v, np.nan)
     e.bufs[S_F] = np.full_like(good_f, np.nan)
+    e.run("setup")
     e.run("prologue")
     e.bufs[vslot] = good_v
     e.bufs[S_F] = good_f
