@@ -159,9 +159,11 @@ ProgInst& get_density(tdcc_system s) {
   auto pi = std::make_unique<ProgInst>();
   pi->prog = std::make_unique<Program>(s->dims, "density");
   build_density(*pi->prog, s->n_mu);
+  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   pi->prog->analyse({});
   pi->bases.assign(pi->prog->slots.size(), nullptr);
-  s->ws_bytes += pi->prog->allocate(pi->bases, s->owned);
+  pi->bytes = pi->prog->allocate(pi->bases, pi->owned);
+  s->ws_bytes += pi->bytes;
   bind_fixed(s, pi->bases);
   s->dens = std::move(pi);
   return *s->dens;
@@ -316,6 +318,10 @@ void reset_programs(tdcc_system s) {
         s->ws_bytes -= pi->bytes;
         pi.reset();
       }
+  if (s->dens) {
+    s->ws_bytes -= s->dens->bytes;
+    s->dens.reset();
+  }
   for (auto& g : s->gexec)
     if (g) {
       cudaGraphExecDestroy(g);

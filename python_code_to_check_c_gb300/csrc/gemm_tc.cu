@@ -31,8 +31,11 @@
 
 #include <cmath>
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 
 #include "engine.h"
 #include "gemm_tc.h"
@@ -492,8 +495,18 @@ static PFN_cuTensorMapEncodeTiled_v12000 encoder() {
   return fn;
 }
 
-// [S][rows_pad][K_pad] BF16, box = (64 K, box_rows rows, 1 slice)
+// [S][rows_pad][K_pad] BF16, box = (64 K, box_rows rows, 1 slice).
+// Encoded maps are cached by (address, layout): a packed buffer keeps its
+// address for the life of its program.
 static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, int box_rows) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, int, int, int>, CUtensorMap> cache;
+  const auto key = std::make_tuple(base, S, rows_pad, K_pad, box_rows);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
   CUtensorMap m;
   cuuint64_t dims[3] = {(cuuint64_t)K_pad, (cuuint64_t)rows_pad, (cuuint64_t)S};
   cuuint64_t strides[2] = {(cuuint64_t)K_pad * 2, (cuuint64_t)K_pad * 2 * rows_pad};
@@ -503,6 +516,8 @@ static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, i
                                es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = m;
   return m;
 }
 

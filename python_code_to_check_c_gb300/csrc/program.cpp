@@ -5,6 +5,7 @@
 // and the per-stage body.
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <stdexcept>
 
 #include "engine.h"
@@ -498,14 +499,37 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
   constexpr int BM = 128, BN = 64, BK = 64;  // tensor-core tile (gemm_tc.h)
   std::vector<Op> out;
   out.reserve(ops.size() * 2);
+  // packed operands already produced: identical packing of an unchanged
+  // source is reused (e.g. t2 with K = (e,f) feeds three contractions)
+  struct PackRef {
+    int slot;
+    long long exp_off;
+    size_t pos;  // index of the pack op in `out`
+    int src;
+  };
+  std::map<std::string, PackRef> pack_cache;
+  std::vector<long long> last_write(slots.size() + 4 * ops.size() + 16, -1);
+  auto push_op = [&](const Op& o) {
+    if (o.write >= 0) {
+      if ((size_t)o.write >= last_write.size()) last_write.resize(o.write + 1, -1);
+      last_write[o.write] = (long long)out.size();
+    }
+    out.push_back(o);
+  };
+  auto group_key = [](const ModeGroup& g, bool use_s1) {
+    std::string k = std::to_string(g.n);
+    for (int i = 0; i < g.n; ++i)
+      k += "," + std::to_string(g.dim[i]) + ":" + std::to_string(use_s1 ? g.s1[i] : g.s0[i]);
+    return k;
+  };
   for (auto& op : ops) {
     if (op.kind != OP_GEMM) {
-      out.push_back(op);
+      push_op(op);
       continue;
     }
     const long long M = op.g.M, N = op.g.N, K = op.g.K;
     if (M * N * K < min_macs || K < min_k) {
-      out.push_back(op);
+      push_op(op);
       continue;
     }
     if (err_slot < 0) {
@@ -532,8 +556,6 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     pa.kind = pb.kind = OP_PACK;
     pa.tag = op.tag + ":packA";
     pb.tag = op.tag + ":packB";
-    pa.pk_dst = packed_slot(op.tag + ":packA", rA, pa.pk_exp_off);
-    pb.pk_dst = packed_slot(op.tag + ":packB", rB, pb.pk_exp_off);
     // A: rows = M modes (strides g.gm.s0), K modes strides g.gk.s0
     pa.pk = PackArgs{};
     pa.pk.cplx = ac;
@@ -565,8 +587,29 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     pb.pk_off = op.ob;
     pb.pk_dt = op.dtb;
     pb.reads = {op.sb};
-    pb.write = pb.pk_dst;
     pb.bytes = N * K * elem_bytes(op.dtb) + (long long)S * rB * Kp * 2;
+    // resolve packed slots (reuse an identical, still valid packing)
+    bool emit_a = true, emit_b = true;
+    auto resolve = [&](Op& pk, const ModeGroup& gr, const ModeGroup& gk, bool k_s1, long long rows,
+                       const std::string& nm, bool& emit) {
+      const std::string key = std::to_string(pk.pk_src) + "@" + std::to_string(pk.pk_off) + "#" +
+                              std::to_string(pk.pk_dt) + "|" + group_key(gr, false) + "|" +
+                              group_key(gk, k_s1) + "|" + std::to_string(rows) + "x" + std::to_string(Kp) +
+                              "s" + std::to_string(S);
+      auto it = pack_cache.find(key);
+      if (it != pack_cache.end() && last_write[it->second.src] < (long long)it->second.pos) {
+        pk.pk_dst = it->second.slot;
+        pk.pk_exp_off = it->second.exp_off;
+        emit = false;
+        return;
+      }
+      pk.pk_dst = packed_slot(nm, rows, pk.pk_exp_off);
+      pk.write = pk.pk_dst;
+      emit = true;
+      pack_cache[key] = PackRef{pk.pk_dst, pk.pk_exp_off, (size_t)-1, pk.pk_src};
+    };
+    resolve(pa, op.g.gm, op.g.gk, false, rA, op.tag + ":packA", emit_a);
+    resolve(pb, op.g.gn, op.g.gk, true, rB, op.tag + ":packB", emit_b);
     // slice product
     t.kind = OP_TCGEMM;
     t.tag = op.tag;
@@ -627,8 +670,12 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     t.reads = {pa.pk_dst, pb.pk_dst};
     if (a.acc || a.atomic) t.reads.push_back(op.sc);
     t.write = op.sc;
-    out.push_back(pa);
-    out.push_back(pb);
+    for (Op* pk : {&pa, &pb}) {
+      if (!((pk == &pa) ? emit_a : emit_b)) continue;
+      for (auto& kv : pack_cache)
+        if (kv.second.slot == pk->pk_dst) kv.second.pos = out.size();
+      push_op(*pk);
+    }
     if (a.atomic && !a.acc) {
       // zero the output first: its modes are the M and N groups (strides s1)
       Op z;
@@ -660,9 +707,9 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
       z.add_oc = op.oc;
       z.write = op.sc;
       z.bytes = M * N * elem_bytes(op.dtc);
-      out.push_back(z);
+      push_op(z);
     }
-    out.push_back(t);
+    push_op(t);
   }
   ops.swap(out);
 }
