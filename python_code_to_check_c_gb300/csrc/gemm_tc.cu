@@ -74,8 +74,11 @@ __global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
   const int m = (int)(warp / kr), k0 = (int)(warp % kr) * 256;
   long long roff;
   decomp_tc(p.gr, m, roff);
-  const double* src = static_cast<const double*>(p.src);
-  double mre = 0.0, mim = 0.0;
+  // max |x| on the bit patterns (for finite doubles the order of |x| is the
+  // order of the unsigned bits with the sign cleared): integer ops only
+  const unsigned long long* src = static_cast<const unsigned long long*>(p.src);
+  constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
+  unsigned long long mre = 0, mim = 0;
 #pragma unroll 4
   for (int j = 0; j < 8; ++j) {
     const int k = k0 + lane + 32 * j;
@@ -84,27 +87,22 @@ __global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
       decomp_tc(p.gk, k, ko);
       const long long e = roff + ko;
       if (p.cplx) {
-        mre = fmax(mre, fabs(src[2 * e]));
-        mim = fmax(mim, fabs(src[2 * e + 1]));
+        mre = max(mre, src[2 * e] & kAbs);
+        mim = max(mim, src[2 * e + 1] & kAbs);
       } else {
-        mre = fmax(mre, fabs(src[e]));
+        mre = max(mre, src[e] & kAbs);
       }
     }
   }
   for (int d = 16; d > 0; d >>= 1) {
-    mre = fmax(mre, __shfl_xor_sync(0xffffffffu, mre, d));
-    mim = fmax(mim, __shfl_xor_sync(0xffffffffu, mim, d));
+    mre = max(mre, __shfl_xor_sync(0xffffffffu, mre, d));
+    mim = max(mim, __shfl_xor_sync(0xffffffffu, mim, d));
   }
   if (lane == 0) {
-    int e;
-    if (mre > 0.0) {
-      frexp(mre, &e);
-      atomicMax(&p.exps[p.cplx ? 2 * m : m], e + kExpBias);
-    }
-    if (p.cplx && mim > 0.0) {
-      frexp(mim, &e);
-      atomicMax(&p.exps[2 * m + 1], e + kExpBias);
-    }
+    // max = f 2^e with f in [0.5, 1): e = biased exponent - 1022
+    const int Ere = (int)(mre >> 52), Eim = (int)(mim >> 52);
+    if (mre != 0) atomicMax(&p.exps[p.cplx ? 2 * m : m], (Ere > 0 ? Ere - 1022 : -1022) + kExpBias);
+    if (p.cplx && mim != 0) atomicMax(&p.exps[2 * m + 1], (Eim > 0 ? Eim - 1022 : -1022) + kExpBias);
   }
 }
 
@@ -362,9 +360,16 @@ __global__ void __launch_bounds__(192, 1)
     // ---------------- epilogue (warps 2..5) ----------------
     const int q = warp & 3;             // TMEM lane quarter this warp may access
     const int row = q * 32 + lane;      // tile row == TMEM lane
-    double acc[TC_BN];
+    // Exact sums in integer units of 2^-u, u = 7 (min(S,5) + 1).  The level
+    // sums are integers (products of integer slices, FP32-exact per chunk),
+    // so sum_L v_L 2^(u - 7L) is exact for S <= 5 (the seventh-slice level of
+    // S = 6 is truncated by 7 bits, below its own resolution) and stays
+    // below 2^52 per chunk: int64 holds up to 2^11 chunks.  No FP64
+    // arithmetic until the final conversion -- the FP64 pipe is narrow.
+    const int u = 7 * ((S < 5 ? S : 5) + 1);
+    long long acc[TC_BN];
 #pragma unroll
-    for (int j = 0; j < TC_BN; ++j) acc[j] = 0.0;
+    for (int j = 0; j < TC_BN; ++j) acc[j] = 0;
     for (int c = 0; c < nchunks; ++c) {
       // warp-uniform decisions: tcgen05.ld and the shuffles below are collective
       if (__any_sync(0xffffffffu, sh->abort != 0)) break;
@@ -374,23 +379,20 @@ __global__ void __launch_bounds__(192, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      // The level sums are integers (products of integer slices); combine
-      // them exactly in 64-bit integers, sum_L v_L 2^(7(S+1-L)) < 2^(24+7(S-1)),
-      // and convert once per chunk (exact for S <= 5).
 #pragma unroll
       for (int j0 = 0; j0 < TC_BN; j0 += 16) {
-        long long comb[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) comb[j] = 0;
         for (int L = 2; L <= S + 1; ++L) {
           float v[16];
           tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((L - 2) * TC_BN + j0), v);
-          const int sh = 7 * (S + 1 - L);
+          const int sh = u - 7 * L;
+          if (sh >= 0) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) comb[j] += __float2ll_rn(v[j]) * (1LL << sh);
+            for (int j = 0; j < 16; ++j) acc[j0 + j] += __float2ll_rn(v[j]) << sh;
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[j0 + j] += __float2ll_rn(v[j]) >> (-sh);
+          }
         }
-#pragma unroll
-        for (int j = 0; j < 16; ++j) acc[j0 + j] += (double)comb[j];
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(smem_u32(&sh->accempty));
@@ -399,11 +401,15 @@ __global__ void __launch_bounds__(192, 1)
       // scale back and write
       const int prow = mt * TC_BM + row;          // packed row of A
       const int ea = prow < g.rowsA_pad ? row_exp(g.expA[prow]) : 0;
+      // converted in place: acc[j] then holds the bits of the FP64 value
 #pragma unroll
       for (int j = 0; j < TC_BN; ++j) {
         const int pcol = nt * TC_BN + j;
-        const int eb = row_exp(g.expB[pcol]);
-        acc[j] = ldexp(acc[j], ea + eb - 7 * (S + 1));
+        const int E = ea + row_exp(g.expB[pcol]) - u;
+        // 2^E built from its bits (one multiply instead of ldexp)
+        const double s2 = (E > -1023 && E < 1024) ? __longlong_as_double((long long)(E + 1023) << 52)
+                                                  : ldexp(1.0, E);
+        acc[j] = __double_as_longlong((double)acc[j] * s2);
       }
       const int m = AC ? (prow >> 1) : prow;
       const bool odd = AC && (lane & 1);
@@ -415,7 +421,7 @@ __global__ void __launch_bounds__(192, 1)
       for (int jj = 0; jj < ncol_log; ++jj) {
         double re, im;
         if constexpr (BC) {
-          const double x0 = acc[2 * jj], x1 = acc[2 * jj + 1];
+          const double x0 = __longlong_as_double(acc[2 * jj]), x1 = __longlong_as_double(acc[2 * jj + 1]);
           if constexpr (AC) {
             const double p0 = __shfl_xor_sync(0xffffffffu, x0, 1);
             const double p1 = __shfl_xor_sync(0xffffffffu, x1, 1);
@@ -428,7 +434,7 @@ __global__ void __launch_bounds__(192, 1)
             im = x1;
           }
         } else {
-          const double x = acc[jj];
+          const double x = __longlong_as_double(acc[jj]);
           if constexpr (AC) {
             const double p = __shfl_xor_sync(0xffffffffu, x, 1);
             re = odd ? p : x;
@@ -445,7 +451,14 @@ __global__ void __launch_bounds__(192, 1)
         long long coffn;
         decomp_tc(g.gnC, n, coffn);
         const long long off = coffm + coffn;
-        const double vr = g.ar * re - g.ai * im, vi = g.ar * im + g.ai * re;
+        double vr, vi;
+        if (g.ai == 0.0) {  // the equations' coefficients are real
+          vr = g.ar * re;
+          vi = g.ar * im;
+        } else {
+          vr = g.ar * re - g.ai * im;
+          vi = g.ar * im + g.ai * re;
+        }
         if (g.cc) {
           if (g.atomic) {
             atomicAdd(&C[off].x, vr);
