@@ -33,6 +33,7 @@ struct ProgInst {
   std::vector<void*> owned;  // this program's workspace allocations
   long long bytes = 0;
   bool setup_done = false;   // integral-only ops (e.g. packed integral blocks) ran
+  DagExec dag;               // streams/events for concurrent execution of the ops
   // runs the integral-only ops once, eagerly, on `st`
   cudaError_t setup(cudaStream_t st) {
     if (setup_done) return cudaSuccess;
@@ -41,7 +42,13 @@ struct ProgInst {
     return e;
   }
   ~ProgInst() {
+    dag.destroy();
     for (void* p : owned) cudaFree(p);
+  }
+  // phase ops as a dependency DAG (serially, in program order, when timed)
+  cudaError_t exec(cudaStream_t st, Program::Phase ph, std::vector<Program::Timed>* timed = nullptr) {
+    if (timed) return prog->run(bases, st, ph, timed);
+    return prog->run_dag(bases, st, ph, dag);
   }
 };
 
@@ -150,6 +157,7 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
   pi->bytes = p.allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;
   bind_fixed(s, pi->bases);
+  pi->dag.init(p.ops.size(), 4);
   slot = std::move(pi);
   return *slot;
 }
@@ -165,6 +173,7 @@ ProgInst& get_density(tdcc_system s) {
   pi->bytes = pi->prog->allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;
   bind_fixed(s, pi->bases);
+  pi->dag.init(pi->prog->ops.size(), 4);
   s->dens = std::move(pi);
   return *s->dens;
 }
@@ -241,13 +250,13 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
   std::vector<Program::Timed> tm;
   B[S_F] = s->Fs;
   CK(pi.setup(st));
-  CK(p.run(B, st, Program::PROLOGUE, pf ? &tm : nullptr));
+  CK(pi.exec(st, Program::PROLOGUE, pf ? &tm : nullptr));
   if (pf) pf->add_prog(tm, b, 0);
   for (int stage = 1; stage <= 4; ++stage) {
     B[S_T1 + b] = stage == 1 ? in[b] : s->yin[b];
     B[S_F] = s->Fs + (stage == 1 ? 0 : stage < 4 ? 1 : 2) * nn;
     tm.clear();
-    CK(p.run(B, st, Program::STAGE, pf ? &tm : nullptr));
+    CK(pi.exec(st, Program::STAGE, pf ? &tm : nullptr));
     if (pf) pf->add_prog(tm, b, stage);
     const double h = stage < 3 ? dt / 2.0 : dt;
     timed_launch(pf, st, "rk4_stage_axpy", b, stage, (double)n * 16 * (stage == 1 ? 3 : stage == 4 ? 3 : 5),
@@ -286,7 +295,7 @@ void run_step(tdcc_system s, int method, double2* const in[4], double2* const ou
   for (int k = 0; k < 4; ++k) d.bases[S_T1 + k] = out[k];
   d.bases[S_RES] = s->res;
   std::vector<Program::Timed> tm;
-  CK(d.prog->run(d.bases, m, Program::ALL, pf ? &tm : nullptr));
+  CK(d.exec(m, Program::ALL, pf ? &tm : nullptr));
   if (pf) pf->add_prog(tm, 4, 0);
   timed_launch(pf, m, "record_mu", 5, 0, 0.0,
                [&] { return launch_record_mu(s->ctx, s->res, s->n_mu, traj, nullptr, m); });
@@ -450,7 +459,7 @@ int tdcc_rhs(tdcc_system s, int method, int block, const void* t1, const void* t
     B[S_F] = const_cast<void*>(F);
     B[S_OUT] = out;
     cudaError_t e = pi.setup(static_cast<cudaStream_t>(stream));
-    if (e == cudaSuccess) e = pi.prog->run(B, static_cast<cudaStream_t>(stream), Program::DYNAMIC);
+    if (e == cudaSuccess) e = pi.exec(static_cast<cudaStream_t>(stream), Program::DYNAMIC);
     if (e != cudaSuccess) return TDCC_ERR_CUDA;
   } catch (const std::exception& ex) {
     return fail(TDCC_ERR_CUDA, ex.what());
@@ -469,7 +478,7 @@ int tdcc_dipole(tdcc_system s, const void* t1, const void* t2, const void* l1, c
     d.bases[S_L1] = const_cast<void*>(l1);
     d.bases[S_L2] = const_cast<void*>(l2);
     d.bases[S_RES] = mu_out;
-    if (d.prog->run(d.bases, static_cast<cudaStream_t>(stream), Program::ALL) != cudaSuccess)
+    if (d.exec(static_cast<cudaStream_t>(stream), Program::ALL) != cudaSuccess)
       return TDCC_ERR_CUDA;
   } catch (const std::exception& ex) {
     return fail(TDCC_ERR_CUDA, ex.what());

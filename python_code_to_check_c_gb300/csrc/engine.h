@@ -188,6 +188,16 @@ struct Dims {  // system sizes
   int o, v, n;
 };
 
+// Streams and per-op events for executing a program as a dependency DAG.
+struct DagExec {
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> ev;     // one per op
+  std::vector<cudaEvent_t> tails;  // one per stream (join)
+  cudaEvent_t fork = nullptr;
+  void init(size_t nops, int nstreams);
+  void destroy();
+};
+
 class Program {
  public:
   Program(Dims dims, std::string name);
@@ -250,6 +260,11 @@ class Program {
   };
   cudaError_t run(const std::vector<void*>& bases, cudaStream_t st, Phase ph,
                   std::vector<Timed>* timed = nullptr) const;
+  // same ops, issued as a DAG over `ex`'s streams (slot hazards become
+  // event edges) and joined back into `st`
+  cudaError_t run_dag(const std::vector<void*>& bases, cudaStream_t st, Phase ph, DagExec& ex) const;
+  cudaError_t launch_op(const Op& op, const std::vector<void*>& bases, cudaStream_t st) const;
+  static bool in_phase(const Op& op, Phase ph);
 
   // mixed precision: which GEMMs go to the tensor-core backend
   // (before analyse/allocate) rewrites every contraction with at least

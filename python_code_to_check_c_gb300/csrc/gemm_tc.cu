@@ -385,12 +385,13 @@ __global__ void __launch_bounds__(192, 1)
           float v[16];
           tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((L - 2) * TC_BN + j0), v);
           const int sh = u - 7 * L;
+          // |v| <= 2^24: a 32-bit conversion is exact and stays off the FP64 pipe
           if (sh >= 0) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j0 + j] += __float2ll_rn(v[j]) << sh;
+            for (int j = 0; j < 16; ++j) acc[j0 + j] += (long long)__float2int_rn(v[j]) << sh;
           } else {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j0 + j] += __float2ll_rn(v[j]) >> (-sh);
+            for (int j = 0; j < 16; ++j) acc[j0 + j] += (long long)__float2int_rn(v[j]) >> (-sh);
           }
         }
       }

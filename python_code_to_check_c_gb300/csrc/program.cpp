@@ -431,62 +431,166 @@ static inline const void* at(const std::vector<void*>& b, int slot, long long of
   return p + off * elem_bytes(dt);
 }
 
+bool Program::in_phase(const Op& op, Phase ph) {
+  switch (ph) {
+    case SETUP: return op.is_const;
+    case DYNAMIC: return !op.is_const;
+    case PROLOGUE: return !op.varying && !op.is_const;
+    case STAGE: return op.varying;
+    default: return true;
+  }
+}
+
+cudaError_t Program::launch_op(const Op& op, const std::vector<void*>& bases, cudaStream_t st) const {
+  cudaError_t e = cudaSuccess;
+  if (op.kind == OP_GEMM) {
+    e = launch_gemm(op, at(bases, op.sa, op.oa, op.dta), at(bases, op.sb, op.ob, op.dtb),
+                    const_cast<void*>(at(bases, op.sc, op.oc, op.dtc)), st);
+  } else if (op.kind == OP_ADD) {
+    AddArgs a = op.a;
+    a.C = const_cast<void*>(at(bases, op.add_sc, op.add_oc, a.cc ? C64 : R64));
+    for (int t = 0; t < a.nt; ++t) {
+      a.t[t].A = at(bases, op.add_slots[t][0], op.add_off[t][0], a.t[t].ac ? C64 : R64);
+      a.t[t].B = op.add_slots[t][1] >= 0
+                     ? at(bases, op.add_slots[t][1], op.add_off[t][1], a.t[t].bc ? C64 : R64)
+                     : nullptr;
+    }
+    e = launch_add(a, st);
+  } else if (op.kind == OP_TRACE) {
+    e = launch_trace(dims.n, dims.o, op.tr_n_mu, static_cast<const double*>(bases[S_MU]),
+                     bases[op.tr_slots[0]], bases[op.tr_slots[1]], bases[op.tr_slots[2]],
+                     bases[op.tr_slots[3]], bases[S_RES], st);
+  } else if (op.kind == OP_PACK) {
+    PackArgs p = op.pk;
+    p.src = at(bases, op.pk_src, op.pk_off, op.pk_dt);
+    char* dst = static_cast<char*>(bases[op.pk_dst]);
+    p.out = dst;
+    p.exps = reinterpret_cast<int*>(dst + op.pk_exp_off);
+    e = launch_pack(p, st);
+  } else if (op.kind == OP_TCGEMM) {
+    TcArgs a = op.tc;
+    const char* pa = static_cast<const char*>(bases[op.tc_pa]);
+    const char* pb = static_cast<const char*>(bases[op.tc_pb]);
+    a.expA = reinterpret_cast<const int*>(pa + op.tc_expa_off);
+    a.expB = reinterpret_cast<const int*>(pb + op.tc_expb_off);
+    a.C = const_cast<void*>(at(bases, op.sc, op.oc, op.dtc));
+    a.err = static_cast<int*>(bases[op.tc_err]);
+    e = launch_ozaki(a, pa, pb, st);
+  }
+  if (e != cudaSuccess) set_error("kernel launch failed in " + op.tag + ": " + cudaGetErrorString(e));
+  return e;
+}
+
 cudaError_t Program::run(const std::vector<void*>& bases, cudaStream_t st, Phase ph,
                          std::vector<Timed>* timed) const {
   for (const auto& op : ops) {
-    if (ph == SETUP && !op.is_const) continue;
-    if (ph == DYNAMIC && op.is_const) continue;
-    if (ph == PROLOGUE && (op.varying || op.is_const)) continue;
-    if (ph == STAGE && !op.varying) continue;
-    cudaError_t e = cudaSuccess;
+    if (!in_phase(op, ph)) continue;
     Timed tm{&op, nullptr, nullptr};
     if (timed) {
       cudaEventCreate(&tm.a);
       cudaEventCreate(&tm.b);
       cudaEventRecord(tm.a, st);
     }
-    if (op.kind == OP_GEMM) {
-      e = launch_gemm(op, at(bases, op.sa, op.oa, op.dta), at(bases, op.sb, op.ob, op.dtb),
-                      const_cast<void*>(at(bases, op.sc, op.oc, op.dtc)), st);
-    } else if (op.kind == OP_ADD) {
-      AddArgs a = op.a;
-      a.C = const_cast<void*>(at(bases, op.add_sc, op.add_oc, a.cc ? C64 : R64));
-      for (int t = 0; t < a.nt; ++t) {
-        a.t[t].A = at(bases, op.add_slots[t][0], op.add_off[t][0], a.t[t].ac ? C64 : R64);
-        a.t[t].B = op.add_slots[t][1] >= 0
-                       ? at(bases, op.add_slots[t][1], op.add_off[t][1], a.t[t].bc ? C64 : R64)
-                       : nullptr;
-      }
-      e = launch_add(a, st);
-    } else if (op.kind == OP_TRACE) {
-      e = launch_trace(dims.n, dims.o, op.tr_n_mu, static_cast<const double*>(bases[S_MU]),
-                       bases[op.tr_slots[0]], bases[op.tr_slots[1]], bases[op.tr_slots[2]],
-                       bases[op.tr_slots[3]], bases[S_RES], st);
-    } else if (op.kind == OP_PACK) {
-      PackArgs p = op.pk;
-      p.src = at(bases, op.pk_src, op.pk_off, op.pk_dt);
-      char* dst = static_cast<char*>(bases[op.pk_dst]);
-      p.out = dst;
-      p.exps = reinterpret_cast<int*>(dst + op.pk_exp_off);
-      e = launch_pack(p, st);
-    } else if (op.kind == OP_TCGEMM) {
-      TcArgs a = op.tc;
-      const char* pa = static_cast<const char*>(bases[op.tc_pa]);
-      const char* pb = static_cast<const char*>(bases[op.tc_pb]);
-      a.expA = reinterpret_cast<const int*>(pa + op.tc_expa_off);
-      a.expB = reinterpret_cast<const int*>(pb + op.tc_expb_off);
-      a.C = const_cast<void*>(at(bases, op.sc, op.oc, op.dtc));
-      a.err = static_cast<int*>(bases[op.tc_err]);
-      e = launch_ozaki(a, pa, pb, st);
-    }
+    const cudaError_t e = launch_op(op, bases, st);
     if (timed) {
       cudaEventRecord(tm.b, st);
       timed->push_back(tm);
     }
-    if (e != cudaSuccess) {
-      set_error("kernel launch failed in " + op.tag + ": " + cudaGetErrorString(e));
-      return e;
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// DAG execution: ops of a phase become nodes; edges follow the slot hazards
+// (read-after-write, write-after-write, write-after-read).  Independent ops
+// go to different streams of the pool; under stream capture the event
+// waits become graph edges, so the captured graph runs them concurrently.
+// ---------------------------------------------------------------------------
+void DagExec::init(size_t nops, int nstreams) {
+  if (!ev.empty()) return;
+  streams.resize(nstreams);
+  for (auto& s : streams) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  ev.resize(nops);
+  for (auto& e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  for (int i = 0; i < nstreams; ++i) {
+    cudaEvent_t e;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    tails.push_back(e);
+  }
+}
+
+void DagExec::destroy() {
+  for (auto& s : streams) cudaStreamDestroy(s);
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (auto& e : tails) cudaEventDestroy(e);
+  if (fork) cudaEventDestroy(fork);
+  streams.clear();
+  ev.clear();
+  tails.clear();
+  fork = nullptr;
+}
+
+cudaError_t Program::run_dag(const std::vector<void*>& bases, cudaStream_t st, Phase ph,
+                             DagExec& ex) const {
+  ex.init(ops.size(), 4);
+  const int ns = (int)ex.streams.size();
+  std::vector<int> last_writer(slots.size(), -1);
+  std::vector<std::vector<int>> readers(slots.size());
+  std::vector<int> op_stream(ops.size(), -1);
+  std::vector<int> tail(ns, -1);  // last op issued on each stream
+  std::vector<char> stream_used(ns, 0);
+  cudaError_t e = cudaEventRecord(ex.fork, st);
+  if (e != cudaSuccess) return e;
+  int rr = 0;
+  for (size_t i = 0; i < ops.size(); ++i) {
+    const Op& op = ops[i];
+    if (!in_phase(op, ph)) continue;
+    std::vector<int> deps;
+    for (int r : op.reads)
+      if (r >= 0 && last_writer[r] >= 0) deps.push_back(last_writer[r]);
+    if (op.write >= 0) {
+      if (last_writer[op.write] >= 0) deps.push_back(last_writer[op.write]);
+      for (int rd : readers[op.write]) deps.push_back(rd);
     }
+    std::sort(deps.begin(), deps.end());
+    deps.erase(std::unique(deps.begin(), deps.end()), deps.end());
+    // prefer the stream whose last op is the newest dependency
+    int s = -1;
+    for (int k = (int)deps.size() - 1; k >= 0 && s < 0; --k)
+      for (int q = 0; q < ns; ++q)
+        if (tail[q] == deps[k]) {
+          s = q;
+          break;
+        }
+    if (s < 0) {
+      s = rr;
+      rr = (rr + 1) % ns;
+    }
+    cudaStream_t cs = ex.streams[s];
+    if (!stream_used[s]) {
+      if ((e = cudaStreamWaitEvent(cs, ex.fork, 0)) != cudaSuccess) return e;
+      stream_used[s] = 1;
+    }
+    for (int d : deps)
+      if (op_stream[d] != s && (e = cudaStreamWaitEvent(cs, ex.ev[d], 0)) != cudaSuccess) return e;
+    if ((e = launch_op(op, bases, cs)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ex.ev[i], cs)) != cudaSuccess) return e;
+    op_stream[i] = s;
+    tail[s] = (int)i;
+    for (int r : op.reads)
+      if (r >= 0) readers[r].push_back((int)i);
+    if (op.write >= 0) {
+      last_writer[op.write] = (int)i;
+      readers[op.write].clear();
+    }
+  }
+  // join every used stream back into the caller's stream
+  for (int q = 0; q < ns; ++q) {
+    if (!stream_used[q]) continue;
+    if ((e = cudaEventRecord(ex.tails[q], ex.streams[q])) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, ex.tails[q], 0)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
