@@ -47,7 +47,12 @@ struct ProgInst {
   }
   // phase ops as a dependency DAG (serially, in program order, when timed)
   cudaError_t exec(cudaStream_t st, Program::Phase ph, std::vector<Program::Timed>* timed = nullptr) {
-    if (timed) return prog->run(bases, st, ph, timed);
+    // TDCC_SERIAL=1 issues every op in program order on `st` (debugging aid)
+    static const bool serial = [] {
+      const char* e = getenv("TDCC_SERIAL");
+      return e && e[0] == '1';
+    }();
+    if (timed || serial) return prog->run(bases, st, ph, timed);
     return prog->run_dag(bases, st, ph, dag);
   }
 };
