@@ -423,6 +423,10 @@ long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned
       throw std::runtime_error("upload of constant slot " + slots[i].name + " failed");
     bytes += (long long)b;
   }
+  // A pageable cudaMemcpy may return before its DMA has landed, and the
+  // program's kernels run on non-blocking streams that do not order against
+  // it: wait for the uploads before any kernel can read these slots.
+  if (cudaDeviceSynchronize() != cudaSuccess) throw std::runtime_error("synchronising constant-slot uploads failed");
   return bytes;
 }
 
