@@ -101,6 +101,22 @@ int tdcc_system_destroy(tdcc_system s);
    the number of BF16 slices per operand (2..6; 7 bits each).             */
 int tdcc_set_precision(tdcc_system s, int mode, int slices);
 
+/* Ground-state amplitudes by Jacobi sweeps with eigh(F) denominators and
+   DIIS, on the device.  Replaces DIIS_solver / DIIS_solver_Lam
+   (CCSD_Helper.py:347-416, 702-776) and DIIS_solver_CC2 /
+   DIIS_solver_Lam_CC2 (CC2_Helper.py:179-248, 324-400) with the same
+   storage pattern (including the CC2 Lambda order, CC2_Helper.py:382).
+   mode 0: T amplitudes, t1/t2 updated in place (l1, l2 may be NULL);
+   mode 1: Lambda amplitudes, l1/l2 updated in place, t1/t2 fixed.
+   eps: HOST double[n], the ascending eigenvalues of the Fock matrix.
+   Stops when |dE| < e_min (the reference's test; it uses 1e-15) or, if
+   r_tol > 0, when a sweep's max |residual| < r_tol, or after maxiter.
+   energy: correlation energy (mode 0) or pseudo-energy E1 + E2 (mode 1).
+   Synchronous; allocates its vector store for the duration of the call. */
+int tdcc_ground_state(tdcc_system s, int method, int mode, void* t1, void* t2, void* l1, void* l2,
+                      const double* eps, int maxsize, int maxiter, double e_min, double r_tol,
+                      double* energy, int* niter, void* stream);
+
 /* Mixed mode routing: contractions with at least min_macs multiply-adds and
    a contracted extent K >= min_k run on the tensor cores (defaults 2^18 and
    32); the rest stay FP64.  (0, 1) sends every contraction to the tensor

@@ -8,7 +8,10 @@
 
 #include "../../include/tdcc.h"
 #include "engine.h"
+#include "ground.h"
 #include "rk4.h"
+
+#include <algorithm>
 
 namespace tdcc {
 
@@ -420,6 +423,232 @@ int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k) {
   reset_programs(s);
   s->tc_min_macs = min_macs;
   s->tc_min_k = min_k;
+  return TDCC_OK;
+}
+
+int tdcc_ground_state(tdcc_system s, int method, int mode, void* t1, void* t2, void* l1, void* l2,
+                      const double* eps_host, int maxsize, int maxiter, double e_min, double r_tol,
+                      double* energy, int* niter, void* stream) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
+  if (mode != 0 && mode != 1) return fail(TDCC_ERR_ARG, "mode must be 0 (T) or 1 (Lambda)");
+  if (!t1 || !t2 || (mode == 1 && (!l1 || !l2)) || !eps_host || !energy || !niter)
+    return fail(TDCC_ERR_ARG, "NULL argument");
+  if (maxsize < 1 || maxsize > 14 || maxiter < 1) return fail(TDCC_ERR_ARG, "need 1 <= maxsize <= 14, maxiter >= 1");
+  std::vector<void*> mem;
+  struct Guard {
+    std::vector<void*>& m;
+    ~Guard() {
+      for (void* p : m) cudaFree(p);
+    }
+  } guard{mem};
+  try {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int o = s->dims.o, v = s->dims.v, n = s->dims.n;
+    const long long n1 = (long long)o * v, n2 = n1 * n1;
+    auto alloc = [&](size_t bytes) {
+      void* p = nullptr;
+      CK(cudaMalloc(&p, bytes));
+      mem.push_back(p);
+      return p;
+    };
+    auto c2 = [&](long long cnt) { return static_cast<double2*>(alloc((size_t)cnt * sizeof(double2))); };
+    double* eps = static_cast<double*>(alloc((size_t)n * sizeof(double)));
+    CK(cudaMemcpyAsync(eps, eps_host, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+    double2* Fc = c2((long long)n * n);
+    CK(g_to_complex(Fc, s->fock, (long long)n * n, st));
+    double2 *r1 = c2(n1), *r2 = c2(n2), *x1 = c2(n1), *x2 = c2(n2), *o1 = c2(n1), *o2 = c2(n2);
+    double2* res = c2(64);
+    const int ns = maxsize + 2, ne = maxsize + 1;
+    std::vector<double2*> S1(ns), S2(ns), E1(ne), E2(ne);
+    for (int k = 0; k < ns; ++k) {
+      S1[k] = c2(n1);
+      S2[k] = c2(n2);
+    }
+    for (int k = 0; k < ne; ++k) {
+      E1[k] = c2(n1);
+      E2[k] = c2(n2);
+    }
+    auto d2d = [&](void* dst, const void* src, long long bytes) {
+      CK(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToDevice, st));
+    };
+    d2d(x1, mode == 0 ? t1 : l1, n1 * 16);
+    d2d(x2, mode == 0 ? t2 : l2, n2 * 16);
+    ProgInst& P1 = get_rhs(s, method, mode == 0 ? TDCC_T1 : TDCC_L1);
+    ProgInst& P2 = get_rhs(s, method, mode == 0 ? TDCC_T2 : TDCC_L2);
+    double last_res = INFINITY;
+    auto rhs = [&](ProgInst& P, double2* out) {
+      auto& B = P.bases;
+      B[S_T1] = mode == 0 ? (void*)x1 : t1;
+      B[S_T2] = mode == 0 ? (void*)x2 : t2;
+      B[S_L1] = mode == 1 ? (void*)x1 : (l1 ? l1 : (void*)x1);
+      B[S_L2] = mode == 1 ? (void*)x2 : (l2 ? l2 : (void*)x2);
+      B[S_F] = Fc;
+      B[S_OUT] = out;
+      CK(P.setup(st));
+      CK(P.exec(st, Program::DYNAMIC));
+    };
+    // one Jacobi sweep: both residuals at the current amplitudes, then update
+    auto update = [&]() {
+      rhs(P1, r1);
+      rhs(P2, r2);
+      if (r_tol > 0.0) {
+        double2 h;
+        CK(g_maxabs(r1, n1, r2, n2, res + 63, st));
+        CK(cudaMemcpyAsync(&h, res + 63, sizeof(h), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        last_res = h.x;
+      }
+      CK(g_jacobi(x1, r1, eps, o, v, 2, n1, st));
+      CK(g_jacobi(x2, r2, eps, o, v, 4, n2, st));
+    };
+    auto energy_of = [&]() {
+      double2 h[2];
+      CK(g_energy(s->tei, s->fock, x1, x2, o, v, mode, res, st));
+      CK(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      return h[0].x + h[1].x;
+    };
+    // buffer bookkeeping for the rolling stores (front = oldest)
+    std::vector<int> s1q, s2q, e1q, e2q, s1free, s2free, efree;
+    for (int k = ns - 1; k >= 0; --k) {
+      s1free.push_back(k);
+      s2free.push_back(k);
+    }
+    for (int k = ne - 1; k >= 0; --k) efree.push_back(k);
+    auto take = [](std::vector<int>& fr) {
+      const int k = fr.back();
+      fr.pop_back();
+      return k;
+    };
+    auto push_s1 = [&](const double2* x) {
+      const int k = take(s1free);
+      d2d(S1[k], x, n1 * 16);
+      s1q.push_back(k);
+    };
+    auto push_s2 = [&](const double2* x) {
+      const int k = take(s2free);
+      d2d(S2[k], x, n2 * 16);
+      s2q.push_back(k);
+    };
+    auto push_e = [&](const double2* a1, const double2* b1, const double2* a2, const double2* b2) {
+      const int k = take(efree);
+      CK(g_sub(E1[k], a1, b1, n1, st));
+      CK(g_sub(E2[k], a2, b2, n2, st));
+      e1q.push_back(k);
+    };
+    // (DIIS_solver, CCSD_Helper.py:347-370): first sweep, then maxsize more
+    update();
+    push_s1(x1);
+    push_s2(x2);
+    for (int k = 1; k <= maxsize; ++k) {
+      update();
+      push_s1(x1);
+      push_s2(x2);
+      push_e(S1[s1q[k]], S1[s1q[k - 1]], S2[s2q[k]], S2[s2q[k - 1]]);
+    }
+    const int m1 = maxsize + 1;
+    std::vector<double> Bm(m1 * m1, -1.0);
+    Bm[m1 * m1 - 1] = 0.0;
+    const bool early_l1 = (method == TDCC_CC2 && mode == 1);  // CC2_Helper.py:382
+    double E = 0.0;
+    int it = 0;
+    for (int z = 1; z < maxiter; ++z) {
+      const double e_old = energy_of();
+      // B[a][b] = <e_b, e_a> (t1 part + t2 part), symmetric
+      std::vector<std::pair<int, int>> pairs;
+      for (int a = 0; a < maxsize; ++a)
+        for (int b = a; b < maxsize; ++b) pairs.push_back({a, b});
+      for (size_t p0 = 0; p0 < pairs.size(); p0 += 32) {
+        DotPairs dp{};
+        const size_t cnt = std::min<size_t>(32, pairs.size() - p0);
+        for (size_t q = 0; q < cnt; ++q) {
+          const int a = pairs[p0 + q].first, b = pairs[p0 + q].second;
+          dp.a[2 * q] = E1[e1q[b]];
+          dp.b[2 * q] = E1[e1q[a]];
+          dp.n[2 * q] = n1;
+          dp.a[2 * q + 1] = E2[e1q[b]];
+          dp.b[2 * q + 1] = E2[e1q[a]];
+          dp.n[2 * q + 1] = n2;
+        }
+        dp.count = (int)(2 * cnt);
+        CK(g_dots(dp, res, st));
+        std::vector<double2> h(2 * cnt);
+        CK(cudaMemcpyAsync(h.data(), res, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (size_t q = 0; q < cnt; ++q) {
+          const int a = pairs[p0 + q].first, b = pairs[p0 + q].second;
+          const double val = h[2 * q].x + h[2 * q + 1].x;
+          Bm[a * m1 + b] = val;
+          Bm[b * m1 + a] = val;
+        }
+      }
+      // solve B c = (0, ..., 0, -1) by Gaussian elimination, partial pivoting
+      std::vector<double> M = Bm, rhsv(m1, 0.0);
+      rhsv[m1 - 1] = -1.0;
+      for (int col = 0; col < m1; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < m1; ++r)
+          if (std::fabs(M[r * m1 + col]) > std::fabs(M[piv * m1 + col])) piv = r;
+        if (M[piv * m1 + col] == 0.0) throw std::runtime_error("singular DIIS matrix");
+        if (piv != col) {
+          for (int c = 0; c < m1; ++c) std::swap(M[col * m1 + c], M[piv * m1 + c]);
+          std::swap(rhsv[col], rhsv[piv]);
+        }
+        for (int r = col + 1; r < m1; ++r) {
+          const double f = M[r * m1 + col] / M[col * m1 + col];
+          for (int c = col; c < m1; ++c) M[r * m1 + c] -= f * M[col * m1 + c];
+          rhsv[r] -= f * rhsv[col];
+        }
+      }
+      std::vector<double> cvec(m1);
+      for (int r = m1 - 1; r >= 0; --r) {
+        double acc = rhsv[r];
+        for (int c = r + 1; c < m1; ++c) acc -= M[r * m1 + c] * cvec[c];
+        cvec[r] = acc / M[r * m1 + r];
+      }
+      // extrapolate x = sum_a c_a stored[a+1]
+      std::vector<const double2*> src1, src2;
+      std::vector<double> coef;
+      for (int a = 0; a < maxsize; ++a) {
+        src1.push_back(S1[s1q[a + 1]]);
+        src2.push_back(S2[s2q[a + 1]]);
+        coef.push_back(cvec[a]);
+      }
+      CK(g_lincomb(x1, src1, coef, n1, st));
+      CK(g_lincomb(x2, src2, coef, n2, st));
+      d2d(o1, x1, n1 * 16);
+      d2d(o2, x2, n2 * 16);
+      E = energy_of();
+      ++it;
+      if (std::fabs(E - e_old) < e_min) break;
+      if (early_l1) {
+        push_s1(x1);
+        update();
+        push_s2(x2);
+      } else {
+        update();
+        push_s1(x1);
+        push_s2(x2);
+      }
+      push_e(x1, o1, x2, o2);
+      s1free.push_back(s1q.front());
+      s1q.erase(s1q.begin());
+      s2free.push_back(s2q.front());
+      s2q.erase(s2q.begin());
+      efree.push_back(e1q.front());
+      e1q.erase(e1q.begin());
+      if (r_tol > 0.0 && last_res < r_tol) break;
+    }
+    d2d(mode == 0 ? t1 : l1, x1, n1 * 16);
+    d2d(mode == 0 ? t2 : l2, x2, n2 * 16);
+    CK(cudaStreamSynchronize(st));
+    *energy = E;
+    *niter = it;
+  } catch (const std::exception& ex) {
+    cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
   return TDCC_OK;
 }
 

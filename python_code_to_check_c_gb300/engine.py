@@ -140,6 +140,40 @@ class CCEngine:
     def L2eq_rhs_CC2(self, t1, t2, l1, l2, F):
         return self.rhs("CC2", TDCC_L2, t1, t2, l1, l2, F)
 
+    # ---- ground state (DIIS on the device) ----
+    def _eps(self, F=None):
+        F = self.fock.detach().cpu().numpy() if F is None else np.asarray(F)
+        return np.ascontiguousarray(np.linalg.eigh(np.real(F))[0], dtype=np.float64)
+
+    def ground_state(self, method: str, mode: int, t1, t2, l1=None, l2=None, maxsize=7, maxiter=40,
+                     E_min=1e-15, r_tol=0.0, F=None):
+        """Jacobi + DIIS on the device; returns (energy, niter, x1, x2) with
+        (x1, x2) = (t1, t2) for mode 0 and (l1, l2) for mode 1."""
+        t1 = to_dev(t1).clone()
+        t2 = to_dev(t2).clone()
+        l1 = to_dev(l1).clone() if l1 is not None else None
+        l2 = to_dev(l2).clone() if l2 is not None else None
+        eps = self._eps(F)
+        e = ctypes.c_double(0.0)
+        it = ctypes.c_int(0)
+        check(self.lib.tdcc_ground_state(self.handle, _lib.METHODS[method], int(mode), _ptr(t1), _ptr(t2),
+                                         _ptr(l1), _ptr(l2), eps.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                         int(maxsize), int(maxiter), float(E_min), float(r_tol),
+                                         ctypes.byref(e), ctypes.byref(it), _stream()),
+              "tdcc_ground_state")
+        return (e.value, it.value) + ((t1, t2) if mode == 0 else (l1, l2))
+
+    def DIIS_solver(self, t1, t2, F=None, maxsize=7, maxiter=40, E_min=1e-15, method="CCSD"):
+        """CCSD_Helper.DIIS_solver (CCSD_Helper.py:347) / DIIS_solver_CC2: returns (E, t1, t2)."""
+        E, _, t1, t2 = self.ground_state(method, 0, t1, t2, maxsize=maxsize, maxiter=maxiter, E_min=E_min, F=F)
+        return E, t1, t2
+
+    def DIIS_solver_Lam(self, t1, t2, l1, l2, F=None, maxsize=7, maxiter=30, E_min=1e-15, method="CCSD"):
+        """CCSD_Helper.DIIS_solver_Lam (CCSD_Helper.py:702) / DIIS_solver_Lam_CC2: (E, l1, l2)."""
+        E, _, l1, l2 = self.ground_state(method, 1, t1, t2, l1, l2, maxsize=maxsize, maxiter=maxiter,
+                                         E_min=E_min, F=F)
+        return E, l1, l2
+
     # ---- density / dipole ----
     def dipole_moment(self, t1, t2, l1, l2, F=None):
         t1, t2, l1, l2 = (to_dev(x) for x in (t1, t2, l1, l2))

@@ -30,9 +30,11 @@ class System:
     v: int
     nq: int
     seed: int
-    B: np.ndarray          # (Q, n, n) float64
+    B: np.ndarray          # (Q, n, n) float64 (None when tei_full is given)
     fock: np.ndarray       # (n, n) float64
     mu: list = field(default_factory=list)   # [mu_x, mu_y, mu_z], each (n, n)
+    tei_full: np.ndarray = None              # explicit <pq||rs> (psi4 systems)
+    scf_energy: float = 0.0
 
     @property
     def n(self) -> int:
@@ -40,6 +42,8 @@ class System:
 
     def tei(self) -> np.ndarray:
         """Antisymmetrised <pq||rs> as an (n,n,n,n) float64 array (host)."""
+        if self.tei_full is not None:
+            return self.tei_full
         return tei_from_df(self.B)
 
     def eps(self) -> np.ndarray:
@@ -68,6 +72,29 @@ def tei_from_df(B: np.ndarray) -> np.ndarray:
     J = (Bm.T @ Bm).reshape(n, n, n, n)          # J[p,r,q,s]
     phys = J.transpose(0, 2, 1, 3)               # [p,q,r,s]
     return np.ascontiguousarray(phys - phys.transpose(0, 1, 3, 2))
+
+
+def system_from_psi4(psi4) -> System:
+    """The integrals CCSD_Helper.__init__ builds from a psi4 SCF
+    (CCSD_Helper.py:26-93, 970-980): spin-orbital <pq||rs> from
+    ``mo_spin_eri``, the MO Fock matrix and the three dipole matrices, spin
+    interleaved (each spatial index p becomes 2p, 2p+1)."""
+    wfn = psi4.scf_helper("SCF", return_wfn=True)
+    scf_e = float(psi4.energy("scf"))
+    mints = psi4.core.MintsHelper(wfn.basisset())
+    mol = psi4.core.get_active_molecule()
+    nmo = wfn.nmo()
+    ndocc = int(sum(mol.Z(a) for a in range(mol.natom())) / 2)
+    C = wfn.Ca()
+    Cn = np.asarray(C)
+    H = np.asarray(mints.ao_kinetic()) + np.asarray(mints.ao_potential())
+    tei = np.asarray(mints.mo_spin_eri(C, C))
+    o = 2 * ndocc
+    spin = lambda X: np.kron(X, np.eye(2))  # noqa: E731
+    fock = spin(Cn.T @ H @ Cn) + np.einsum("pmqm->pq", tei[:, :o, :, :o])
+    mu = [spin(Cn.T @ np.asarray(d) @ Cn) for d in mints.so_dipole()]
+    return System(o=o, v=2 * nmo - o, nq=0, seed=-1, B=None, fock=fock, mu=mu, tei_full=tei,
+                  scf_energy=scf_e)
 
 
 def mp2_guess(tei: np.ndarray, eps: np.ndarray, o: int) -> np.ndarray:
