@@ -97,6 +97,28 @@ int tdcc_system_create(int o, int v, const double* tei, const double* fock,
                        const double* mu, int n_mu, tdcc_system* out);
 int tdcc_system_destroy(tdcc_system s);
 
+/* A system that advances nb (1..1024) trajectories over the same integrals
+   together; no counterpart in the reference, which runs one trajectory per
+   process.  Every per-trajectory array of the other entry points then holds
+   nb copies back to back ([nb][...]): t1/t2/l1/l2 and their outputs, the
+   dressed Fock matrix of tdcc_rhs ([nb][n][n]), mu_out ([nb][n_mu]) and the
+   trajectories of tdcc_propagate ([nsteps][nb]).  Contractions with an
+   integral operand run once for all trajectories (the trajectory index
+   joins the GEMM's row or column modes); products of two per-trajectory
+   operands run as batched products.  tdcc_ground_state needs nb = 1 (make
+   a single-trajectory system over the same integrals for it).             */
+int tdcc_system_create_batched(int o, int v, const double* tei, const double* fock,
+                               const double* mu, int n_mu, int nb, tdcc_system* out);
+int tdcc_system_batch(tdcc_system s);   /* nb of the system (0 for NULL) */
+
+/* Per-trajectory fields for tdcc_rk4_step / tdcc_propagate called with
+   field = NULL: fields (HOST tdcc_field[nb]) and pol (HOST int[nb], the
+   dipole component 0..n_mu-1 each field couples to and whose expectation
+   value tdcc_propagate records; NULL = the last component).  fields = NULL
+   clears them.  A non-NULL field argument overrides them: that field for
+   every trajectory, along the last component.                             */
+int tdcc_set_fields(tdcc_system s, const tdcc_field* fields, const int* pol);
+
 /* Selects the contraction arithmetic (TDCC_PREC_*) and, for the mixed mode,
    the number of BF16 slices per operand (2..6; 7 bits each).             */
 int tdcc_set_precision(tdcc_system s, int mode, int slices);
@@ -160,7 +182,8 @@ int tdcc_dipole(tdcc_system s, const void* t1, const void* t2, const void* l1,
    t = t_prev + dt, t + dt/2, t + dt (the reference advances t first).
    The new state round(old, precs) + delta is written to the *_out arrays
    (which may alias the inputs).  If mu_out is not NULL the dipole of the
-   new state is written there (complex128[n_mu]).                          */
+   new state is written there (complex128[nb][n_mu]).  field: see
+   tdcc_set_fields.                                                        */
 int tdcc_rk4_step(tdcc_system s, int method, const void* t1, const void* t2,
                   const void* l1, const void* l2, void* t1_out, void* t2_out,
                   void* l1_out, void* l2_out, double t_prev, double dt, int precs,
@@ -168,9 +191,11 @@ int tdcc_rk4_step(tdcc_system s, int method, const void* t1, const void* t2,
 
 /* nsteps RK4 steps with the state resident on the device and the step
    captured once in a CUDA graph.  The state arrays are read at entry and
-   overwritten with the final state.  mu_traj (device complex128[nsteps])
-   receives mu_z after every step.  Synchronous: returns after the last
-   step completed (TDCC_ERR_NONFINITE if the final state is not finite).   */
+   overwritten with the final state.  mu_traj (device complex128[nsteps][nb])
+   receives after every step each trajectory's dipole component along its
+   field (mu_z for a single trajectory).  Synchronous: returns after the
+   last step completed (TDCC_ERR_NONFINITE if a final dipole is not
+   finite).                                                                */
 int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void* l2,
                    double t0, double dt, int nsteps, int precs,
                    const tdcc_field* field, void* mu_traj, void* stream);
@@ -195,12 +220,13 @@ int tdcc_dipole_noalloc(int o, int v, const void* t1, const void* t2, const void
                         void* stream);
 
 /* Writes a JSON description of the op list that computes (method, block)
-   for sizes (o, v): buffer slots, and per op the GEMM mode groups / strides
-   or the elementwise terms, plus whether the op runs once per RK4 step or
-   in every stage.  block = 4 selects the density / dipole program.  Needs no
-   GPU (used by the CPU tests to check the programs; no counterpart in the
-   reference).  Returns the JSON length; TDCC_ERR_LIMIT if buf is too small.*/
-long long tdcc_program_json(int o, int v, int method, int block, int n_mu, char* buf,
+   for sizes (o, v) and nb trajectories: buffer slots, and per op the GEMM
+   mode groups / strides / batch strides or the elementwise terms, plus
+   whether the op runs once per RK4 step or in every stage.  block = 4
+   selects the density / dipole program.  Needs no GPU (used by the CPU
+   tests to check the programs; no counterpart in the reference).  Returns
+   the JSON length; TDCC_ERR_LIMIT if buf is too small.                    */
+long long tdcc_program_json(int o, int v, int method, int block, int n_mu, int nb, char* buf,
                             size_t len);
 
 /* Per-kernel timing record of tdcc_profile_step. */

@@ -60,6 +60,9 @@ SIGNATURES = {
     "tdcc_launch_count": (_ll, []),
     "tdcc_system_create": (_i, [_i, _i, _vp, _vp, _vp, _i, ctypes.POINTER(_vp)]),
     "tdcc_system_destroy": (_i, [_vp]),
+    "tdcc_system_create_batched": (_i, [_i, _i, _vp, _vp, _vp, _i, _i, ctypes.POINTER(_vp)]),
+    "tdcc_system_batch": (_i, [_vp]),
+    "tdcc_set_fields": (_i, [_vp, ctypes.POINTER(TdccField), ctypes.POINTER(_i)]),
     "tdcc_set_precision": (_i, [_vp, _i, _i]),
     "tdcc_workspace_bytes": (_ll, [_vp]),
     "tdcc_check_errors": (_i, [_vp]),
@@ -73,7 +76,7 @@ SIGNATURES = {
     "tdcc_propagate": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _d, _i, _i,
                             ctypes.POINTER(TdccField), _vp, _vp]),
     "tdcc_dipole_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
-    "tdcc_program_json": (_ll, [_i, _i, _i, _i, _i, ctypes.c_char_p, ctypes.c_size_t]),
+    "tdcc_program_json": (_ll, [_i, _i, _i, _i, _i, _i, ctypes.c_char_p, ctypes.c_size_t]),
     "tdcc_profile_step": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _d, _i, ctypes.POINTER(TdccField),
                                ctypes.POINTER(TdccOpRecord), _i, ctypes.POINTER(_i)]),
 }
@@ -115,15 +118,15 @@ def check(rc: int, what: str = "") -> None:
         raise TdccError(f"{what} failed with code {rc}: {last_error()}")
 
 
-def program_json(o: int, v: int, method: str, block: int, n_mu: int = 3) -> dict:
-    """The op list libtdcc runs for (method, block) at sizes (o, v), as a dict
-    (block 4 = density / dipole).  Works without a GPU."""
+def program_json(o: int, v: int, method: str, block: int, n_mu: int = 3, nb: int = 1) -> dict:
+    """The op list libtdcc runs for (method, block) at sizes (o, v) and nb
+    trajectories, as a dict (block 4 = density / dipole).  Works without a GPU."""
     import json
     lib = load()
     cap = 1 << 20
     while True:
         buf = ctypes.create_string_buffer(cap)
-        n = lib.tdcc_program_json(o, v, METHODS[method], block, n_mu, buf, cap)
+        n = lib.tdcc_program_json(o, v, METHODS[method], block, n_mu, nb, buf, cap)
         if n >= 0:
             return json.loads(buf.value.decode())
         if n != -6:

@@ -80,6 +80,9 @@ struct tdcc_system_s {
   long long tc_min_macs = kTcMinMacs;  // tensor-core routing policy
   int tc_min_k = kTcMinK;
   int device = 0;
+  int nb = 1;                       // trajectories advanced together
+  std::vector<tdcc_field> h_fields; // per-trajectory fields (tdcc_set_fields)
+  std::vector<int> h_pol;
   std::unique_ptr<ProgInst> rhs[2][4];
   std::unique_ptr<ProgInst> dens;
   std::vector<void*> owned;
@@ -88,7 +91,10 @@ struct tdcc_system_s {
   // RK4 machinery
   bool rk_ready = false;
   StepCtx* ctx = nullptr;          // device
-  double2* Fs = nullptr;           // 3 x n x n dressed Fock matrices
+  tdcc_field* d_fields = nullptr;  // device [nb]
+  int* d_pol = nullptr;            // device [nb]
+  double2* d_E = nullptr;          // device [nb][3]
+  double2* Fs = nullptr;           // 3 x nb x n x n dressed Fock matrices
   double2* kbuf[4] = {};
   double2* acc[4] = {};
   double2* yin[4] = {};
@@ -104,10 +110,12 @@ struct tdcc_system_s {
   double2* g_traj = nullptr;
   long long g_nodes[2] = {0, 0};   // kernel nodes per captured step graph
 
+  // elements of block b for one trajectory / for all trajectories
   long long nel(int b) const {
     const long long o = dims.o, v = dims.v;
     return (b == TDCC_T1 || b == TDCC_L1) ? o * v : o * o * v * v;
   }
+  long long nelb(int b) const { return nel(b) * nb; }
 };
 
 namespace {
@@ -158,6 +166,7 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
     build_l1_cc2(p);
   else
     build_l2_cc2(p, p.ones("ones_v", s->dims.v));
+  p.batch(s->nb);
   p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
@@ -175,6 +184,7 @@ ProgInst& get_density(tdcc_system s) {
   auto pi = std::make_unique<ProgInst>();
   pi->prog = std::make_unique<Program>(s->dims, "density");
   build_density(*pi->prog, s->n_mu);
+  pi->prog->batch(s->nb);
   pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   pi->prog->analyse({});
   pi->bases.assign(pi->prog->slots.size(), nullptr);
@@ -190,16 +200,19 @@ void ensure_rk(tdcc_system s) {
   if (s->rk_ready) return;
   const long long n = s->dims.n;
   s->ctx = static_cast<StepCtx*>(dalloc(s, sizeof(StepCtx)));
-  s->Fs = static_cast<double2*>(dalloc(s, 3 * n * n * sizeof(double2)));
+  s->d_fields = static_cast<tdcc_field*>(dalloc(s, s->nb * sizeof(tdcc_field)));
+  s->d_pol = static_cast<int*>(dalloc(s, s->nb * sizeof(int)));
+  s->d_E = static_cast<double2*>(dalloc(s, 3 * s->nb * sizeof(double2)));
+  s->Fs = static_cast<double2*>(dalloc(s, 3 * s->nb * n * n * sizeof(double2)));
   for (int b = 0; b < 4; ++b) {
-    const size_t bytes = s->nel(b) * sizeof(double2);
+    const size_t bytes = s->nelb(b) * sizeof(double2);
     s->kbuf[b] = static_cast<double2*>(dalloc(s, bytes));
     s->acc[b] = static_cast<double2*>(dalloc(s, bytes));
     s->yin[b] = static_cast<double2*>(dalloc(s, bytes));
     s->st[0][b] = static_cast<double2*>(dalloc(s, bytes));
     s->st[1][b] = static_cast<double2*>(dalloc(s, bytes));
   }
-  s->res = static_cast<double2*>(dalloc(s, 4 * sizeof(double2)));
+  s->res = static_cast<double2*>(dalloc(s, (size_t)s->nb * s->n_mu * sizeof(double2)));
   CK(cudaStreamCreateWithFlags(&s->main, cudaStreamNonBlocking));
   for (int b = 0; b < 4; ++b) {
     CK(cudaStreamCreateWithFlags(&s->bs[b], cudaStreamNonBlocking));
@@ -253,8 +266,8 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
   auto& B = pi.bases;
   for (int k = 0; k < 4; ++k) B[S_T1 + k] = in[k];
   B[S_OUT] = s->kbuf[b];
-  const long long n = s->nel(b);
-  const long long nn = (long long)s->dims.n * s->dims.n;
+  const long long n = s->nelb(b);
+  const long long nn = (long long)s->dims.n * s->dims.n * s->nb;  // one stage's dressed Fock matrices
   std::vector<Program::Timed> tm;
   B[S_F] = s->Fs;
   CK(pi.setup(st));
@@ -284,10 +297,9 @@ void run_step(tdcc_system s, int method, double2* const in[4], double2* const ou
               int precs, double2* traj, Prof* pf = nullptr) {
   cudaStream_t m = s->main;
   const long long nn = (long long)s->dims.n * s->dims.n;
-  timed_launch(pf, m, "advance_field", 5, 0, 0.0, [&] { return launch_advance_field(s->ctx, m); });
-  const double* muz = s->mu + (long long)(s->n_mu - 1) * nn;
-  timed_launch(pf, m, "dress_fock", 5, 0, (double)nn * (8 + 8 + 3 * 16),
-               [&] { return launch_dress(s->ctx, s->fock, muz, s->Fs, s->dims.n, m); });
+  timed_launch(pf, m, "advance_field", 5, 0, 0.0, [&] { return launch_advance_field(s->ctx, s->nb, m); });
+  timed_launch(pf, m, "dress_fock", 5, 0, (double)nn * (8 + 8 * s->nb + 3 * 16 * s->nb),
+               [&] { return launch_dress(s->ctx, s->fock, s->mu, s->Fs, s->dims.n, s->nb, m); });
   if (pf) {
     for (int b = 0; b < 4; ++b) run_block(s, method, b, in, out[b], dt, precs, m, pf);
   } else {
@@ -306,17 +318,39 @@ void run_step(tdcc_system s, int method, double2* const in[4], double2* const ou
   CK(d.exec(m, Program::ALL, pf ? &tm : nullptr));
   if (pf) pf->add_prog(tm, 4, 0);
   timed_launch(pf, m, "record_mu", 5, 0, 0.0,
-               [&] { return launch_record_mu(s->ctx, s->res, s->n_mu, traj, nullptr, m); });
+               [&] { return launch_record_mu(s->ctx, s->res, s->nb, traj, nullptr, m); });
 }
 
+// Time, step counter and the trajectories' fields: `f` for every trajectory
+// (along the last dipole component) when given, else the fields of
+// tdcc_set_fields, else no field.
 void set_ctx(tdcc_system s, double t, double dt, const tdcc_field* f, cudaStream_t st) {
   StepCtx h;
   memset(&h, 0, sizeof(h));
   h.t = t;
   h.dt = dt;
-  if (f) h.field = *f;
   h.step = 0;
+  h.nb = s->nb;
+  h.n_mu = s->n_mu;
+  h.fields = s->d_fields;
+  h.pol = s->d_pol;
+  h.E = s->d_E;
+  std::vector<tdcc_field> fl(s->nb);
+  std::vector<int> pol(s->nb, s->n_mu - 1);
+  if (f) {
+    for (auto& x : fl) x = *f;
+  } else if ((int)s->h_fields.size() == s->nb) {
+    fl = s->h_fields;
+    pol = s->h_pol;
+  } else {
+    for (auto& x : fl) {
+      memset(&x, 0, sizeof(x));
+      x.kind = TDCC_FIELD_NONE;
+    }
+  }
   CK(cudaMemcpyAsync(s->ctx, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s->d_fields, fl.data(), fl.size() * sizeof(tdcc_field), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s->d_pol, pol.data(), pol.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));
 }
 
@@ -365,7 +399,13 @@ long long tdcc_launch_count(void) { return launch_count(); }
 
 int tdcc_system_create(int o, int v, const double* tei, const double* fock, const double* mu,
                        int n_mu, tdcc_system* out) {
+  return tdcc_system_create_batched(o, v, tei, fock, mu, n_mu, 1, out);
+}
+
+int tdcc_system_create_batched(int o, int v, const double* tei, const double* fock, const double* mu,
+                               int n_mu, int nb, tdcc_system* out) {
   if (!out) return fail(TDCC_ERR_ARG, "out is NULL");
+  if (nb < 1 || nb > kMaxTrajectories) return fail(TDCC_ERR_ARG, "nb must be 1..1024");
   *out = nullptr;
   if (o < 1 || v < 1) return fail(TDCC_ERR_ARG, "o and v must be >= 1");
   if ((long long)(o + v) * (o + v) * (o + v) * (o + v) >= (1LL << 40))
@@ -378,8 +418,34 @@ int tdcc_system_create(int o, int v, const double* tei, const double* fock, cons
   s->fock = fock;
   s->mu = mu;
   s->n_mu = n_mu;
+  s->nb = nb;
   cudaGetDevice(&s->device);
   *out = s;
+  return TDCC_OK;
+}
+
+int tdcc_system_batch(tdcc_system s) { return s ? s->nb : 0; }
+
+int tdcc_set_fields(tdcc_system s, const tdcc_field* fields, const int* pol) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!fields) {
+    s->h_fields.clear();
+    s->h_pol.clear();
+    return TDCC_OK;
+  }
+  std::vector<int> p(s->nb, s->n_mu - 1);
+  for (int b = 0; b < s->nb; ++b) {
+    if (fields[b].kind < TDCC_FIELD_NONE || fields[b].kind > TDCC_FIELD_ENVELOPE)
+      return fail(TDCC_ERR_ARG, "bad field kind for trajectory " + std::to_string(b));
+    if (fields[b].n_env < 0 || fields[b].n_env > TDCC_MAX_ENVELOPE)
+      return fail(TDCC_ERR_ARG, "bad envelope size for trajectory " + std::to_string(b));
+    if (pol) {
+      if (pol[b] < 0 || pol[b] >= s->n_mu) return fail(TDCC_ERR_ARG, "polarisation out of range");
+      p[b] = pol[b];
+    }
+  }
+  s->h_fields.assign(fields, fields + s->nb);
+  s->h_pol = p;
   return TDCC_OK;
 }
 
@@ -435,6 +501,8 @@ int tdcc_ground_state(tdcc_system s, int method, int mode, void* t1, void* t2, v
   if (!t1 || !t2 || (mode == 1 && (!l1 || !l2)) || !eps_host || !energy || !niter)
     return fail(TDCC_ERR_ARG, "NULL argument");
   if (maxsize < 1 || maxsize > 14 || maxiter < 1) return fail(TDCC_ERR_ARG, "need 1 <= maxsize <= 14, maxiter >= 1");
+  if (s->nb != 1)
+    return fail(TDCC_ERR_STATE, "ground state needs a single-trajectory system (nb = 1) over the same integrals");
   std::vector<void*> mem;
   struct Guard {
     std::vector<void*>& m;
@@ -741,8 +809,10 @@ int tdcc_rk4_step(tdcc_system s, int method, const void* t1, const void* t2, con
     run_step(s, method, in, tmp, dt, precs, nullptr);
     void* outs[4] = {t1_out, t2_out, l1_out, l2_out};
     for (int b = 0; b < 4; ++b)
-      CK(cudaMemcpyAsync(outs[b], tmp[b], s->nel(b) * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
-    if (mu_out) CK(cudaMemcpyAsync(mu_out, s->res, s->n_mu * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
+      CK(cudaMemcpyAsync(outs[b], tmp[b], s->nelb(b) * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
+    if (mu_out)
+      CK(cudaMemcpyAsync(mu_out, s->res, (size_t)s->nb * s->n_mu * sizeof(double2), cudaMemcpyDeviceToDevice,
+                         s->main));
     CK(cudaEventRecord(s->ev_user, s->main));
     CK(cudaStreamWaitEvent(user, s->ev_user, 0));
   } catch (const std::exception& ex) {
@@ -767,7 +837,7 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
     CK(cudaStreamWaitEvent(s->main, s->ev_user, 0));
     void* st_user[4] = {t1, t2, l1, l2};
     for (int b = 0; b < 4; ++b)
-      CK(cudaMemcpyAsync(s->st[0][b], st_user[b], s->nel(b) * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
+      CK(cudaMemcpyAsync(s->st[0][b], st_user[b], s->nelb(b) * sizeof(double2), cudaMemcpyDeviceToDevice, s->main));
     set_ctx(s, t0, dt, field, s->main);
     // (re)capture the two ping-pong step graphs when the configuration changed
     if (s->g_method != method || s->g_dt != dt || s->g_precs != precs || s->g_prec_mode != s->prec_mode ||
@@ -822,13 +892,16 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
     }
     const int fin = nsteps & 1;
     for (int b = 0; b < 4; ++b)
-      CK(cudaMemcpyAsync(st_user[b], s->st[fin][b], s->nel(b) * sizeof(double2), cudaMemcpyDeviceToDevice, user));
+      CK(cudaMemcpyAsync(st_user[b], s->st[fin][b], s->nelb(b) * sizeof(double2), cudaMemcpyDeviceToDevice, user));
     CK(cudaStreamSynchronize(user));
     if (nsteps > 0) {
-      double2 last;
-      CK(cudaMemcpy(&last, (double2*)mu_traj + (nsteps - 1), sizeof(last), cudaMemcpyDeviceToHost));
-      if (!std::isfinite(last.x) || !std::isfinite(last.y))
-        return fail(TDCC_ERR_NONFINITE, "dipole is not finite after propagation");
+      std::vector<double2> last(s->nb);
+      CK(cudaMemcpy(last.data(), (double2*)mu_traj + (long long)(nsteps - 1) * s->nb, s->nb * sizeof(double2),
+                    cudaMemcpyDeviceToHost));
+      for (int b = 0; b < s->nb; ++b)
+        if (!std::isfinite(last[b].x) || !std::isfinite(last[b].y))
+          return fail(TDCC_ERR_NONFINITE, "dipole of trajectory " + std::to_string(b) +
+                                              " is not finite after propagation");
     }
   } catch (const std::exception& ex) {
     return fail(TDCC_ERR_CUDA, ex.what());
@@ -890,7 +963,7 @@ int tdcc_profile_step(tdcc_system s, int method, const void* t1, const void* t2,
 // ---------------------------------------------------------------------------
 namespace {
 
-void build_program(Program& p, int method, int block, int n_mu) {
+void build_program(Program& p, int method, int block, int n_mu, int nb = 1) {
   if (block == 4)
     build_density(p, n_mu);
   else if (block == TDCC_T1)
@@ -907,6 +980,7 @@ void build_program(Program& p, int method, int block, int n_mu) {
     build_l1_cc2(p);
   else
     build_l2_cc2(p, p.ones("ones_v", p.dims.v));
+  p.batch(nb);
   if (block == 4)
     p.analyse({});
   else
@@ -938,7 +1012,8 @@ std::string program_json(const Program& p) {
   for (size_t i = 0; i < p.slots.size(); ++i) {
     const auto& s = p.slots[i];
     j += (i ? "," : "") + std::string("{\"name\":\"") + s.name + "\",\"dt\":" + std::to_string(s.dt) +
-         ",\"numel\":" + std::to_string(s.numel) + ",\"fixed\":" + (s.fixed ? "true" : "false") +
+         ",\"numel\":" + std::to_string(s.numel) + ",\"numel1\":" + std::to_string(s.numel1) +
+         ",\"batched\":" + (s.batched ? "true" : "false") + ",\"fixed\":" + (s.fixed ? "true" : "false") +
          ",\"ones\":" + (s.init.empty() ? "false" : "true") + "}";
   }
   j += "],\"ops\":[";
@@ -956,24 +1031,29 @@ std::string program_json(const Program& p) {
            ",\"M\":" + std::to_string(g.M) + ",\"N\":" + std::to_string(g.N) + ",\"K\":" + std::to_string(g.K) +
            ",\"gm\":" + jgroup(g.gm) + ",\"gn\":" + jgroup(g.gn) + ",\"gk\":" + jgroup(g.gk) +
            ",\"ar\":" + jnum(g.ar) + ",\"ai\":" + jnum(g.ai) + ",\"acc\":" + std::to_string(g.acc) +
-           ",\"atomic\":" + std::to_string(g.atomic) + ",\"flops\":" + std::to_string(op.flops) + "}";
+           ",\"atomic\":" + std::to_string(g.atomic) + ",\"nsplit\":" + std::to_string(g.nsplit) +
+           ",\"kchunk\":" + std::to_string(g.kchunk) + ",\"nb\":" + std::to_string(g.nb) +
+           ",\"bsA\":" + std::to_string(g.bsA) + ",\"bsB\":" + std::to_string(g.bsB) +
+           ",\"bsC\":" + std::to_string(g.bsC) + ",\"flops\":" + std::to_string(op.flops) + "}";
     } else if (op.kind == OP_ADD) {
       const AddArgs& a = op.a;
       j += "{\"kind\":\"add\",\"varying\":" + var + ",\"sc\":" + std::to_string(op.add_sc) +
            ",\"oc\":" + std::to_string(op.add_oc) + ",\"cc\":" + std::to_string(a.cc) +
-           ",\"acc\":" + std::to_string(a.acc) + ",\"d\":" + jarr(a.d, 4) + ",\"sC\":" + jarr(a.sC, 4) + ",\"terms\":[";
+           ",\"acc\":" + std::to_string(a.acc) + ",\"d\":" + jarr(a.d, a.nd) + ",\"sC\":" + jarr(a.sC, a.nd) +
+           ",\"terms\":[";
       for (int t = 0; t < a.nt; ++t) {
         const AddTerm& T = a.t[t];
         j += (t ? "," : "") + std::string("{\"sa\":") + std::to_string(op.add_slots[t][0]) +
              ",\"oa\":" + std::to_string(op.add_off[t][0]) + ",\"ac\":" + std::to_string(T.ac) +
-             ",\"sA\":" + jarr(T.sA, 4) + ",\"sb\":" + std::to_string(op.add_slots[t][1]) +
+             ",\"sA\":" + jarr(T.sA, a.nd) + ",\"sb\":" + std::to_string(op.add_slots[t][1]) +
              ",\"ob\":" + std::to_string(op.add_off[t][1]) + ",\"bc\":" + std::to_string(T.bc) +
-             ",\"sB\":" + jarr(T.sB, 4) + ",\"cr\":" + jnum(T.cr) + ",\"ci\":" + jnum(T.ci) + "}";
+             ",\"sB\":" + jarr(T.sB, a.nd) + ",\"cr\":" + jnum(T.cr) + ",\"ci\":" + jnum(T.ci) + "}";
       }
       j += "]}";
     } else {
       j += "{\"kind\":\"trace\",\"varying\":" + var + ",\"slots\":" + jarr(op.tr_slots, 4) +
-           ",\"n_mu\":" + std::to_string(op.tr_n_mu) + "}";
+           ",\"n_mu\":" + std::to_string(op.tr_n_mu) + ",\"nb\":" + std::to_string(op.tr_nb) +
+           ",\"bs\":" + jarr(op.tr_bs, 4) + ",\"bsres\":" + std::to_string(op.tr_bsres) + "}";
     }
   }
   return j + "]}";
@@ -981,13 +1061,13 @@ std::string program_json(const Program& p) {
 
 }  // namespace
 
-extern "C" long long tdcc_program_json(int o, int v, int method, int block, int n_mu, char* buf,
+extern "C" long long tdcc_program_json(int o, int v, int method, int block, int n_mu, int nb, char* buf,
                                        size_t len) {
-  if (o < 1 || v < 1 || !valid_method(method) || block < 0 || block > 4 || n_mu < 1 || n_mu > 3)
+  if (o < 1 || v < 1 || !valid_method(method) || block < 0 || block > 4 || n_mu < 1 || n_mu > 3 || nb < 1)
     return fail(TDCC_ERR_ARG, "bad arguments");
   try {
     Program p(Dims{o, v, o + v}, "introspect");
-    build_program(p, method, block, n_mu);
+    build_program(p, method, block, n_mu, nb);
     const std::string j = program_json(p);
     if (!buf || len < j.size() + 1) return fail(TDCC_ERR_LIMIT, "buffer too small: need " + std::to_string(j.size() + 1));
     memcpy(buf, j.c_str(), j.size() + 1);

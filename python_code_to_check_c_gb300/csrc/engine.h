@@ -18,7 +18,7 @@ inline long long elem_bytes(int dt) { return dt == C64 ? 16 : dt == R64 ? 8 : 1;
 // ---------------------------------------------------------------------------
 // Kernel argument blocks (passed by value to the kernels)
 // ---------------------------------------------------------------------------
-constexpr int kMaxModes = 3;
+constexpr int kMaxModes = 4;
 
 // A group of tensor modes flattened into one GEMM dimension.  s0/s1 are the
 // element strides of each mode in the two tensors that carry the group
@@ -38,25 +38,32 @@ struct GemmArgs {
   ModeGroup gm, gn, gk;
   double ar, ai;   // alpha
   int acc;         // C += alpha*AB (else C = alpha*AB)
-  int kchunk;      // K range per blockIdx.z
+  int kchunk;      // K range per split
   int atomic;      // split-K: accumulate with atomics (C pre-initialised)
+  int nsplit;      // K splits; blockIdx.z = batch * nsplit + split
+  int nb;          // batch count (independent products, one per trajectory)
+  long long bsA, bsB, bsC;  // batch strides in elements (0: shared operand)
 };
 
 constexpr int kMaxAddTerms = 6;
+constexpr int kAddDims = 6;
 
 struct AddTerm {
   const void* A;   // never null
   const void* B;   // optional second factor (elementwise product), may be null
-  long long sA[4];
-  long long sB[4];
+  long long sA[kAddDims];
+  long long sB[kAddDims];
   int ac, bc;      // A / B complex?
   double cr, ci;   // coefficient
 };
 
+// Elementwise iteration space: nd dimensions (last fastest), merged where
+// every operand is contiguous across neighbours.
 struct AddArgs {
   void* C;
-  long long sC[4];
-  int d[4];
+  int nd;
+  long long sC[kAddDims];
+  int d[kAddDims];
   long long total;
   int cc;          // C complex?
   int acc;         // C += sum (else C = sum)
@@ -113,18 +120,23 @@ struct PackArgs {
   int cplx;
   ModeGroup gr;      // row modes, strides in s0 (elements of src)
   ModeGroup gk;      // K modes, strides in s0
-  int rows;          // logical rows (M or N)
+  int rows;          // logical rows (M or N) per batch
   int K;
-  int rows_pad;      // packed rows (x2 for complex), multiple of the tile
+  int rows_pad;      // packed rows per batch (x2 for complex), multiple of the tile
   int K_pad;         // multiple of the K tile
   int S;             // slices
-  void* out;         // [S][rows_pad][K_pad] BF16
-  int* exps;         // [rows_pad]
+  int nb;            // batches: packed rows of batch z start at z * rows_pad
+  long long bs;      // batch stride of src in elements
+  void* out;         // [S][nb * rows_pad][K_pad] BF16
+  int* exps;         // [nb * rows_pad]
 };
 
 struct TcArgs {
-  int M, N;                 // logical output extents
-  int rowsA_pad, rowsB_pad; // packed rows
+  int M, N;                 // logical output extents (per batch)
+  int rowsA_pad, rowsB_pad; // packed rows per batch
+  int nb, nsplit;           // blockIdx.z = batch * nsplit + split
+  int bat_a, bat_b;         // A / B packed per batch (else shared by all batches)
+  long long bsC;            // output batch stride in elements
   int kblocks, kb_per_split;
   int S;
   int tmem_cols;
@@ -150,6 +162,7 @@ struct Op {
   GemmArgs g{};
   int backend = GB_FP64;
   int tile = 0;            // FP64 tile shape index (kTiles)
+  bool zeroed = false;     // C is zeroed (or accumulated into) before: split-K allowed
   long long flops = 0;     // real flops of this contraction
   long long bytes = 0;     // compulsory bytes read + written
   // ADD
@@ -161,6 +174,9 @@ struct Op {
   // TRACE: res[k] = sum over 4 density blocks of mu_k * rho (see kernels)
   int tr_slots[4];
   int tr_n_mu = 0;
+  int tr_nb = 1;           // trajectories; strides of the four density blocks and of res
+  long long tr_bs[4] = {0, 0, 0, 0};
+  long long tr_bsres = 0;
   // PACK: operand slot/offset/type -> packed slot (exponents at pk_exp_off bytes)
   PackArgs pk{};
   int pk_src = -1, pk_dt = R64, pk_dst = -1;
@@ -179,9 +195,11 @@ struct Op {
 struct SlotInfo {
   std::string name;
   int dt;
-  long long numel;
+  long long numel;           // all trajectories (numel1 * nb when batched)
   bool fixed;
   std::vector<double> init;  // uploaded at allocation (constant slots)
+  bool batched = false;      // one copy per trajectory, [nb][numel1]
+  long long numel1 = 0;      // elements of one copy (the batch stride)
 };
 
 struct Dims {  // system sizes
@@ -212,7 +230,7 @@ class Program {
   View G(const char* blk) const;             // TEI block, e.g. "oovv"
   View Fb(const char* blk) const;            // dressed Fock block "ov"
   View amp(int slot) const;                  // T1/T2/L1/L2 view
-  View out(int nd) const;                    // output view (o,v) or (o,o,v,v)
+  View out(int nd);                          // output view (o,v) or (o,o,v,v)
 
   // workspace tensor of the given shape ('o'/'v' letters), contiguous
   View ws(const std::string& nm, const char* shape, int dt = C64);
@@ -244,6 +262,17 @@ class Program {
   // marks ops that (transitively) read one of the varying slots
   void analyse(const std::vector<int>& varying_slots);
 
+  // Runs the program for nb trajectories at once (before select_backend):
+  // slots that depend on the per-trajectory inputs (F, amplitudes, output,
+  // result) get nb copies, [nb][numel]; contractions with one shared operand
+  // fold the trajectory index into M or N, the others become batched
+  // products; elementwise ops gain an outer trajectory dimension.
+  void batch(int nb);
+  int nb = 1;
+  long long bstride(int slot) const { return slots[slot].batched ? slots[slot].numel1 : 0; }
+  // tile shape and split-K of a contraction from its extents
+  static void plan_gemm(Op& op, bool allow_split);
+
   // device allocation of workspace slots (returns bytes allocated)
   long long allocate(std::vector<void*>& bases, std::vector<void*>& owned);
 
@@ -274,6 +303,9 @@ class Program {
   int err_slot = -1;  // U8 slot holding the tensor-core kernels' error flag
 };
 
+// merges contiguous dimensions of an elementwise op (program.cpp)
+void coalesce(AddArgs& a);
+
 // FP64 contraction tile shapes (kernels.cu)
 constexpr int kNumTiles = 5;
 extern const int kTiles[kNumTiles][2];
@@ -286,8 +318,8 @@ cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, 
 bool tc_available();
 cudaError_t launch_add(const AddArgs& a, cudaStream_t st);
 cudaError_t launch_trace(int n, int o, int n_mu, const double* mu, const void* dij,
-                         const void* l1, const void* dai, const void* dab, void* res,
-                         cudaStream_t st);
+                         const void* l1, const void* dai, const void* dab, void* res, int nb,
+                         const long long* bs, long long bsres, cudaStream_t st);
 void count_launch(long long k = 1);
 long long launch_count();
 

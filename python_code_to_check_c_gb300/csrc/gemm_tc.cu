@@ -70,10 +70,13 @@ __global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int kr = (p.K + 255) / 256;
-  if (warp >= (long long)p.rows * kr) return;
-  const int m = (int)(warp / kr), k0 = (int)(warp % kr) * 256;
+  if (warp >= (long long)p.rows * p.nb * kr) return;
+  const long long rg = warp / kr;  // logical row over all batches
+  const int z = (int)(rg / p.rows), m = (int)(rg % p.rows), k0 = (int)(warp % kr) * 256;
   long long roff;
   decomp_tc(p.gr, m, roff);
+  roff += z * p.bs;
+  int* exps = p.exps + (size_t)z * p.rows_pad;
   // max |x| on the bit patterns (for finite doubles the order of |x| is the
   // order of the unsigned bits with the sign cleared): integer ops only
   const unsigned long long* src = static_cast<const unsigned long long*>(p.src);
@@ -101,8 +104,8 @@ __global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
   if (lane == 0) {
     // max = f 2^e with f in [0.5, 1): e = biased exponent - 1022
     const int Ere = (int)(mre >> 52), Eim = (int)(mim >> 52);
-    if (mre != 0) atomicMax(&p.exps[p.cplx ? 2 * m : m], (Ere > 0 ? Ere - 1022 : -1022) + kExpBias);
-    if (p.cplx && mim != 0) atomicMax(&p.exps[2 * m + 1], (Eim > 0 ? Eim - 1022 : -1022) + kExpBias);
+    if (mre != 0) atomicMax(&exps[p.cplx ? 2 * m : m], (Ere > 0 ? Ere - 1022 : -1022) + kExpBias);
+    if (p.cplx && mim != 0) atomicMax(&exps[2 * m + 1], (Eim > 0 ? Eim - 1022 : -1022) + kExpBias);
   }
 }
 
@@ -123,16 +126,20 @@ __device__ __forceinline__ unsigned long long fixed_point(double x, int e, int n
 // 7S bits and cut into S signed 7-bit digits (|q_s| <= 127, exact in BF16):
 //   x 2^-e ~= sum_s q_s 2^(-7s).   Zero in the padding.
 __global__ void __launch_bounds__(256) pack_slice_kernel(const PackArgs p) {
-  const int pr = blockIdx.x;
+  const int prg = blockIdx.x;             // packed row over all batches
+  const int z = prg / p.rows_pad, pr = prg - z * p.rows_pad;
   const int m = p.cplx ? (pr >> 1) : pr;
   __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
   const double* src = static_cast<const double*>(p.src);
-  const size_t plane = (size_t)p.rows_pad * p.K_pad;
-  const size_t rowbase = (size_t)pr * p.K_pad;
+  const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
+  const size_t rowbase = (size_t)prg * p.K_pad;
   const bool live = m < p.rows;
   long long ro = 0;
-  if (live) decomp_tc(p.gr, m, ro);
-  const int e = row_exp(p.exps[pr]);
+  if (live) {
+    decomp_tc(p.gr, m, ro);
+    ro += z * p.bs;
+  }
+  const int e = row_exp(p.exps[prg]);
   const int nbits = 7 * p.S;
   for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < p.K_pad; k += gridDim.y * blockDim.x) {
     unsigned long long f = 0ull;
@@ -276,7 +283,10 @@ __global__ void __launch_bounds__(192, 1)
   const uint32_t tmem = sh->tmem;
 
   const int mt = blockIdx.y, nt = blockIdx.x;
-  const int kb0 = blockIdx.z * g.kb_per_split;
+  const int zb = blockIdx.z / g.nsplit;                 // batch
+  const int kb0 = (blockIdx.z - zb * g.nsplit) * g.kb_per_split;
+  const int rowA0 = (g.bat_a ? zb * g.rowsA_pad : 0);  // packed-row origin of this batch
+  const int rowB0 = (g.bat_b ? zb * g.rowsB_pad : 0);
   const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
   const int nkb = kb1 - kb0;
   const int nchunks = (nkb + TC_CHUNK_KB - 1) / TC_CHUNK_KB;
@@ -295,8 +305,8 @@ __global__ void __launch_bounds__(192, 1)
           }
           const uint32_t fb = smem_u32(&sh->full[st]);
           mbar_expect_tx(fb, TC_A_BYTES + TC_B_BYTES);
-          tma3d(smem_u32(stA + st * TC_A_BYTES), &tmA, kb * TC_BK, mt * TC_BM, s, fb);
-          tma3d(smem_u32(stB + st * TC_B_BYTES), &tmB, kb * TC_BK, nt * TC_BN, s, fb);
+          tma3d(smem_u32(stA + st * TC_A_BYTES), &tmA, kb * TC_BK, rowA0 + mt * TC_BM, s, fb);
+          tma3d(smem_u32(stB + st * TC_B_BYTES), &tmB, kb * TC_BK, rowB0 + nt * TC_BN, s, fb);
         }
       // drain: every issued load must land before the CTA exits
       const int issued = it;
@@ -400,13 +410,13 @@ __global__ void __launch_bounds__(192, 1)
     }
     if (!__any_sync(0xffffffffu, sh->abort != 0)) {
       // scale back and write
-      const int prow = mt * TC_BM + row;          // packed row of A
-      const int ea = prow < g.rowsA_pad ? row_exp(g.expA[prow]) : 0;
+      const int prow = mt * TC_BM + row;          // packed row of A (within the batch)
+      const int ea = prow < g.rowsA_pad ? row_exp(g.expA[rowA0 + prow]) : 0;
       // converted in place: acc[j] then holds the bits of the FP64 value
 #pragma unroll
       for (int j = 0; j < TC_BN; ++j) {
         const int pcol = nt * TC_BN + j;
-        const int E = ea + row_exp(g.expB[pcol]) - u;
+        const int E = ea + row_exp(g.expB[rowB0 + pcol]) - u;
         // 2^E built from its bits (one multiply instead of ldexp)
         const double s2 = (E > -1023 && E < 1024) ? __longlong_as_double((long long)(E + 1023) << 52)
                                                   : ldexp(1.0, E);
@@ -416,7 +426,7 @@ __global__ void __launch_bounds__(192, 1)
       const bool odd = AC && (lane & 1);
       long long coffm = 0;
       if (m < g.M) decomp_tc(g.gmC, m, coffm);
-      double2* C = static_cast<double2*>(g.C);
+      double2* C = static_cast<double2*>(g.C) + (g.cc ? zb * g.bsC : 0);
       constexpr int ncol_log = BC ? TC_BN / 2 : TC_BN;  // logical output columns in this tile
 #pragma unroll
       for (int jj = 0; jj < ncol_log; ++jj) {
@@ -473,7 +483,7 @@ __global__ void __launch_bounds__(192, 1)
             C[off] = make_double2(vr, vi);
           }
         } else {
-          double* Cr = static_cast<double*>(g.C);
+          double* Cr = static_cast<double*>(g.C) + zb * g.bsC;
           if (g.atomic)
             atomicAdd(&Cr[off], vr);
           else if (g.acc)
@@ -536,16 +546,17 @@ static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, i
 }
 
 cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(p.exps, 0, (size_t)p.rows_pad * sizeof(int), st);
+  if (p.nb < 1) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(p.exps, 0, (size_t)p.nb * p.rows_pad * sizeof(int), st);
   if (e != cudaSuccess) return e;
-  const long long warps = (long long)p.rows * ((p.K + 255) / 256);
+  const long long warps = (long long)p.rows * p.nb * ((p.K + 255) / 256);
   if (warps > 0) {
     pack_rowmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(p);
     count_launch();
   }
   const int threads = p.K_pad >= 256 ? 256 : p.K_pad;
   const int by = (p.K_pad + threads - 1) / threads > 8 ? 8 : (p.K_pad + threads - 1) / threads;
-  pack_slice_kernel<<<dim3(p.rows_pad, by), threads, 0, st>>>(p);
+  pack_slice_kernel<<<dim3((unsigned)((long long)p.nb * p.rows_pad), by), threads, 0, st>>>(p);
   count_launch();
   return cudaGetLastError();
 }
@@ -567,9 +578,10 @@ cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, 
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  const CUtensorMap ma = slice_map(packA, a.S, a.rowsA_pad, a.kblocks * TC_BK, TC_BM);
-  const CUtensorMap mb = slice_map(packB, a.S, a.rowsB_pad, a.kblocks * TC_BK, TC_BN);
-  dim3 grid(a.rowsB_pad / TC_BN, a.rowsA_pad / TC_BM, (a.kblocks + a.kb_per_split - 1) / a.kb_per_split);
+  if (a.nb < 1 || a.nsplit < 1 || (long long)a.nsplit * a.kb_per_split < a.kblocks) return cudaErrorInvalidValue;
+  const CUtensorMap ma = slice_map(packA, a.S, (a.bat_a ? a.nb : 1) * a.rowsA_pad, a.kblocks * TC_BK, TC_BM);
+  const CUtensorMap mb = slice_map(packB, a.S, (a.bat_b ? a.nb : 1) * a.rowsB_pad, a.kblocks * TC_BK, TC_BN);
+  dim3 grid(a.rowsB_pad / TC_BN, a.rowsA_pad / TC_BM, (unsigned)((long long)a.nb * a.nsplit));
   if (a.ac && a.bc)
     ozaki_kernel<true, true><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
   else if (a.ac)

@@ -87,11 +87,13 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
   const int tid = threadIdx.x;
   const int tx = tid % RX, ty = tid / RX;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int kbeg = blockIdx.z * g.kchunk;
+  const int zb = blockIdx.z / g.nsplit;          // batch
+  const int ks = blockIdx.z - zb * g.nsplit;     // K split
+  const int kbeg = ks * g.kchunk;
   const int kend = min(g.K, kbeg + g.kchunk);
 
-  const TA* A = static_cast<const TA*>(g.A);
-  const TB* B = static_cast<const TB*>(g.B);
+  const TA* A = static_cast<const TA*>(g.A) + zb * g.bsA;
+  const TB* B = static_cast<const TB*>(g.B) + zb * g.bsB;
 
   // this thread's load row (A) / column (B) and their base offsets
   const int ar = tid % BM, ak0 = tid / BM;
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
       const double2 s = acc[i][j];
       const long long off = coffm[i] + coffn[j];
       if constexpr (CC) {
-        double2* C = static_cast<double2*>(g.C);
+        double2* C = static_cast<double2*>(g.C) + zb * g.bsC;
         const double2 v = make_double2(g.ar * s.x - g.ai * s.y, g.ar * s.y + g.ai * s.x);
         if (g.atomic) {
           atomicAdd(&C[off].x, v.x);
@@ -187,7 +189,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
           C[off] = v;
         }
       } else {
-        double* C = static_cast<double*>(g.C);
+        double* C = static_cast<double*>(g.C) + zb * g.bsC;
         const double v = g.ar * s.x;
         if (g.atomic)
           atomicAdd(&C[off], v);
@@ -237,8 +239,11 @@ cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cud
   g.C = C;
   const int bm = kTiles[op.tile][0], bn = kTiles[op.tile][1];
   const int gx = (g.N + bn - 1) / bn, gy = (g.M + bm - 1) / bm;
-  const int gz = (g.K + g.kchunk - 1) / g.kchunk;
-  dim3 grid(gx, gy, gz);
+  if (g.nb < 1) g.nb = 1;
+  if (g.nsplit < 1) g.nsplit = 1;
+  if ((long long)g.nsplit * g.kchunk < g.K) return cudaErrorInvalidValue;
+  const long long gz = (long long)g.nb * g.nsplit;
+  dim3 grid(gx, gy, (unsigned)gz);
   if (gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
   const bool ac = op.dta == C64, bc = op.dtb == C64, cc = op.dtc == C64;
   if (ac && bc)
@@ -263,30 +268,45 @@ __device__ __forceinline__ double2 ld(const void* p, long long off, int cplx) {
   return make_double2(static_cast<const double*>(p)[off], 0.0);
 }
 
+template <typename IDX>
 __global__ void __launch_bounds__(256) add_kernel(const AddArgs a) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < a.total; idx += stride) {
-    long long l = idx;
-    const int i3 = (int)(l % a.d[3]);
-    l /= a.d[3];
-    const int i2 = (int)(l % a.d[2]);
-    l /= a.d[2];
-    const int i1 = (int)(l % a.d[1]);
-    const int i0 = (int)(l / a.d[1]);
+  const IDX stride = (IDX)gridDim.x * blockDim.x;
+  for (IDX idx = (IDX)blockIdx.x * blockDim.x + threadIdx.x; idx < (IDX)a.total; idx += stride) {
+    // decode the (coalesced) index, last dimension fastest
+    IDX l = idx;
+    int ii[kAddDims];
+#pragma unroll
+    for (int q = kAddDims - 1; q >= 0; --q) {
+      ii[q] = 0;
+      if (q < a.nd) {
+        const IDX d = (IDX)a.d[q];
+        ii[q] = (int)(l % d);
+        l /= d;
+      }
+    }
     double2 s = cz();
     for (int t = 0; t < a.nt; ++t) {
       const AddTerm& T = a.t[t];
-      const long long oa = i0 * T.sA[0] + i1 * T.sA[1] + i2 * T.sA[2] + i3 * T.sA[3];
+      long long oa = 0, ob = 0;
+#pragma unroll
+      for (int q = 0; q < kAddDims; ++q) {
+        if (q < a.nd) {
+          oa += (long long)ii[q] * T.sA[q];
+          ob += (long long)ii[q] * T.sB[q];
+        }
+      }
       double2 x = ld(T.A, oa, T.ac);
       if (T.B) {
-        const long long ob = i0 * T.sB[0] + i1 * T.sB[1] + i2 * T.sB[2] + i3 * T.sB[3];
         const double2 y = ld(T.B, ob, T.bc);
         x = make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
       }
       s.x += T.cr * x.x - T.ci * x.y;
       s.y += T.cr * x.y + T.ci * x.x;
     }
-    const long long oc = i0 * a.sC[0] + i1 * a.sC[1] + i2 * a.sC[2] + i3 * a.sC[3];
+    long long oc = 0;
+#pragma unroll
+    for (int q = 0; q < kAddDims; ++q)
+      if (q < a.nd) oc += (long long)ii[q] * a.sC[q];
     if (a.cc) {
       double2* C = static_cast<double2*>(a.C);
       if (a.acc) {
@@ -306,14 +326,24 @@ __global__ void __launch_bounds__(256) add_kernel(const AddArgs a) {
 
 cudaError_t launch_add(const AddArgs& a, cudaStream_t st) {
   if (a.total <= 0) return cudaSuccess;
+  if (a.nd < 1 || a.nd > kAddDims) return cudaErrorInvalidValue;
   long long blocks = (a.total + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  add_kernel<<<(unsigned)blocks, 256, 0, st>>>(a);
+  // 32-bit index arithmetic unless the index space needs 64 bits
+  if (a.total + (long long)blocks * 256 < (1LL << 32))
+    add_kernel<unsigned><<<(unsigned)blocks, 256, 0, st>>>(a);
+  else
+    add_kernel<unsigned long long><<<(unsigned)blocks, 256, 0, st>>>(a);
   count_launch();
   return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
+struct TraceBatch {
+  long long bs[4];  // batch strides of Dij, l1, Dai, Dab (elements)
+  long long bsres;
+};
+
 // dipole trace: res[k] = sum_ij mu_k[i,j] rho[i,j], rho = [[Dij, l1],[Dai, Dab]]
 // One CTA per dipole component; warp-shuffle + shared-memory reduction, so
 // the sum order is fixed (deterministic).
@@ -321,8 +351,14 @@ cudaError_t launch_add(const AddArgs& a, cudaStream_t st) {
 __global__ void __launch_bounds__(1024) trace_kernel(int n, int o, const double* mu,
                                                      const double2* dij, const double2* l1,
                                                      const double2* dai, const double2* dab,
-                                                     double2* res) {
+                                                     double2* res, TraceBatch tb) {
   const int k = blockIdx.x;
+  const int z = blockIdx.y;  // trajectory
+  dij += z * tb.bs[0];
+  l1 += z * tb.bs[1];
+  dai += z * tb.bs[2];
+  dab += z * tb.bs[3];
+  res += z * tb.bsres;
   const int v = n - o;
   const double* M = mu + (long long)k * n * n;
   double sr = 0.0, si = 0.0;
@@ -366,11 +402,16 @@ __global__ void __launch_bounds__(1024) trace_kernel(int n, int o, const double*
 }
 
 cudaError_t launch_trace(int n, int o, int n_mu, const double* mu, const void* dij, const void* l1,
-                         const void* dai, const void* dab, void* res, cudaStream_t st) {
-  trace_kernel<<<n_mu, 1024, 0, st>>>(n, o, mu, static_cast<const double2*>(dij),
-                                      static_cast<const double2*>(l1),
-                                      static_cast<const double2*>(dai),
-                                      static_cast<const double2*>(dab), static_cast<double2*>(res));
+                         const void* dai, const void* dab, void* res, int nb, const long long* bs,
+                         long long bsres, cudaStream_t st) {
+  TraceBatch tb;
+  for (int k = 0; k < 4; ++k) tb.bs[k] = nb > 1 ? bs[k] : 0;
+  tb.bsres = nb > 1 ? bsres : 0;
+  trace_kernel<<<dim3(n_mu, nb > 1 ? nb : 1), 1024, 0, st>>>(n, o, mu, static_cast<const double2*>(dij),
+                                                             static_cast<const double2*>(l1),
+                                                             static_cast<const double2*>(dai),
+                                                             static_cast<const double2*>(dab),
+                                                             static_cast<double2*>(res), tb);
   count_launch();
   return cudaGetLastError();
 }

@@ -87,9 +87,10 @@ View Program::amp(int slot) const {
   return x;
 }
 
-View Program::out(int nd) const {
+View Program::out(int nd) {
   View x = amp(nd == 2 ? S_T1 : S_T2);
   x.slot = S_OUT;
+  slots[S_OUT].numel = x.numel();  // the per-trajectory extent (batch stride)
   return x;
 }
 
@@ -219,21 +220,8 @@ void Program::ein(const char* spec, double ar, double ai, const View& A, const V
   g.ar = ar;
   g.ai = ai;
   g.acc = acc ? 1 : 0;
-  // tile shape, then split-K so that few output tiles still fill the 152 SMs
-  op.tile = choose_tile(M, N);
-  const long long tiles = ((M + kTiles[op.tile][0] - 1) / kTiles[op.tile][0]) *
-                          ((N + kTiles[op.tile][1] - 1) / kTiles[op.tile][1]);
-  long long splits = 1;
-  if (tiles < 2 * 152 && K >= 64) {
-    splits = (2 * 152 + tiles - 1) / tiles;
-    splits = std::min<long long>(splits, K / 32);
-    splits = std::max<long long>(splits, 1);
-  }
-  long long kchunk = (K + splits - 1) / splits;
-  kchunk = ((kchunk + 15) / 16) * 16;
-  g.kchunk = (int)std::max<long long>(kchunk, 16);
-  splits = (K + g.kchunk - 1) / g.kchunk;
-  g.atomic = splits > 1 ? 1 : 0;
+  g.nb = 1;
+  plan_gemm(op, true);
   op.sa = A.slot;
   op.sb = B.slot;
   op.sc = C.slot;
@@ -254,11 +242,36 @@ void Program::ein(const char* spec, double ar, double ai, const View& A, const V
   if (acc) op.reads.push_back(C.slot);
   op.write = C.slot;
   // split-K accumulates with atomics: zero the target first when overwriting
+  op.zeroed = acc;
   if (g.atomic && !acc) {
     zero(C);
     op.reads.push_back(C.slot);
+    op.zeroed = true;
   }
   ops.push_back(op);
+}
+
+// Tile shape, then split-K so that few output tiles still fill the 152 SMs
+// (only where the output is zeroed or accumulated into: splits add with
+// atomics).
+void Program::plan_gemm(Op& op, bool allow_split) {
+  GemmArgs& g = op.g;
+  const long long M = g.M, N = g.N, K = g.K, nbt = std::max(g.nb, 1);
+  op.tile = choose_tile(M, N);
+  const long long tiles = ((M + kTiles[op.tile][0] - 1) / kTiles[op.tile][0]) *
+                          ((N + kTiles[op.tile][1] - 1) / kTiles[op.tile][1]) * nbt;
+  long long splits = 1;
+  if (allow_split && tiles < 2 * 152 && K >= 64) {
+    splits = (2 * 152 + tiles - 1) / tiles;
+    splits = std::min<long long>(splits, K / 32);
+    splits = std::max<long long>(splits, 1);
+  }
+  long long kchunk = (K + splits - 1) / splits;
+  kchunk = ((kchunk + 15) / 16) * 16;
+  g.kchunk = (int)std::max<long long>(kchunk, 16);
+  splits = (K + g.kchunk - 1) / g.kchunk;
+  g.nsplit = (int)std::max<long long>(splits, 1);
+  g.atomic = splits > 1 ? 1 : 0;
 }
 
 void Program::add(const View& C, bool acc, const std::vector<Term>& terms) {
@@ -268,17 +281,11 @@ void Program::add(const View& C, bool acc, const std::vector<Term>& terms) {
   op.tag = name + ":add";
   AddArgs& a = op.a;
   memset(&a, 0, sizeof(a));
-  for (int i = 0; i < 4; ++i) {
-    a.d[i] = i < C.nd ? C.d[i] : 1;
-    a.sC[i] = i < C.nd ? C.s[i] : 0;
-  }
-  // right-align so the last index is the fastest (C.nd may be < 4)
-  if (C.nd < 4) {
-    const int sh = 4 - C.nd;
-    for (int i = 3; i >= 0; --i) {
-      a.d[i] = i - sh >= 0 ? C.d[i - sh] : 1;
-      a.sC[i] = i - sh >= 0 ? C.s[i - sh] : 0;
-    }
+  if (C.nd > kAddDims) throw std::runtime_error("add: too many dimensions in " + name);
+  a.nd = C.nd;
+  for (int i = 0; i < C.nd; ++i) {
+    a.d[i] = C.d[i];
+    a.sC[i] = C.s[i];
   }
   a.total = C.numel();
   a.cc = C.dt == C64;
@@ -288,7 +295,6 @@ void Program::add(const View& C, bool acc, const std::vector<Term>& terms) {
   op.add_oc = C.off;
   op.write = C.slot;
   if (acc) op.reads.push_back(C.slot);
-  const int sh = 4 - C.nd;
   for (int t = 0; t < a.nt; ++t) {
     const Term& T = terms[t];
     if (T.A.nd != C.nd) throw std::runtime_error("add: term rank mismatch in " + name);
@@ -298,14 +304,14 @@ void Program::add(const View& C, bool acc, const std::vector<Term>& terms) {
     at.cr = T.cr;
     at.ci = T.ci;
     at.ac = T.A.dt == C64;
-    for (int i = 0; i < 4; ++i) at.sA[i] = i - sh >= 0 ? T.A.s[i - sh] : 0;
+    for (int i = 0; i < C.nd; ++i) at.sA[i] = T.A.s[i];
     op.add_slots[t][0] = T.A.slot;
     op.add_off[t][0] = T.A.off;
     op.reads.push_back(T.A.slot);
     if (T.B.slot >= 0) {
       if (T.B.nd != C.nd) throw std::runtime_error("add: factor rank mismatch in " + name);
       at.bc = T.B.dt == C64;
-      for (int i = 0; i < 4; ++i) at.sB[i] = i - sh >= 0 ? T.B.s[i - sh] : 0;
+      for (int i = 0; i < C.nd; ++i) at.sB[i] = T.B.s[i];
       op.add_slots[t][1] = T.B.slot;
       op.add_off[t][1] = T.B.off;
       op.reads.push_back(T.B.slot);
@@ -323,7 +329,61 @@ void Program::add(const View& C, bool acc, const std::vector<Term>& terms) {
       if (op.add_slots[t][1] >= 0) ++nread;
     op.bytes = a.total * e * (nread + 1);
   }
+  coalesce(a);
   ops.push_back(op);
+}
+
+// Drops unit dimensions and merges neighbours k, k+1 wherever every operand
+// is contiguous across them (s[k] == s[k+1] * d[k+1]), so the kernel
+// decodes as few indices as possible.
+void coalesce(AddArgs& a) {
+  int nd = 0;
+  int d[kAddDims];
+  long long sc[kAddDims], sa[kMaxAddTerms][kAddDims], sb[kMaxAddTerms][kAddDims];
+  for (int i = 0; i < a.nd; ++i) {
+    if (a.d[i] == 1) continue;
+    const bool merge = nd > 0 && [&] {
+      const int j = nd - 1;
+      if (sc[j] != a.sC[i] * a.d[i]) return false;
+      for (int t = 0; t < a.nt; ++t) {
+        if (sa[t][j] != a.t[t].sA[i] * a.d[i]) return false;
+        if (sb[t][j] != a.t[t].sB[i] * a.d[i]) return false;
+      }
+      return true;
+    }();
+    if (merge) {
+      const int j = nd - 1;
+      d[j] *= a.d[i];
+      sc[j] = a.sC[i];
+      for (int t = 0; t < a.nt; ++t) {
+        sa[t][j] = a.t[t].sA[i];
+        sb[t][j] = a.t[t].sB[i];
+      }
+    } else {
+      d[nd] = a.d[i];
+      sc[nd] = a.sC[i];
+      for (int t = 0; t < a.nt; ++t) {
+        sa[t][nd] = a.t[t].sA[i];
+        sb[t][nd] = a.t[t].sB[i];
+      }
+      ++nd;
+    }
+  }
+  if (nd == 0) {  // a single element
+    d[0] = 1;
+    sc[0] = 0;
+    for (int t = 0; t < a.nt; ++t) sa[t][0] = sb[t][0] = 0;
+    nd = 1;
+  }
+  a.nd = nd;
+  for (int i = 0; i < kAddDims; ++i) {
+    a.d[i] = i < nd ? d[i] : 1;
+    a.sC[i] = i < nd ? sc[i] : 0;
+    for (int t = 0; t < a.nt; ++t) {
+      a.t[t].sA[i] = i < nd ? sa[t][i] : 0;
+      a.t[t].sB[i] = i < nd ? sb[t][i] : 0;
+    }
+  }
 }
 
 void Program::trace(int n_mu, const View& Dij, const View& L1, const View& Dai, const View& Dab) {
@@ -335,6 +395,7 @@ void Program::trace(int n_mu, const View& Dij, const View& L1, const View& Dai, 
   op.tr_slots[2] = Dai.slot;
   op.tr_slots[3] = Dab.slot;
   op.tr_n_mu = n_mu;
+  slots[S_RES].numel = n_mu;  // res = [n_mu] per trajectory
   op.reads = {Dij.slot, L1.slot, Dai.slot, Dab.slot, S_MU};
   op.write = S_RES;
   ops.push_back(op);
@@ -405,6 +466,116 @@ void Program::analyse(const std::vector<int>& varying_slots) {
   for (size_t i = 0; i < ops.size(); ++i) ops[i].is_const = !opdyn[i];
 }
 
+// ---------------------------------------------------------------------------
+// trajectory batching
+// ---------------------------------------------------------------------------
+static bool prepend_mode(ModeGroup& g, int dim, long long s0, long long s1) {
+  if (g.n >= kMaxModes) return false;
+  for (int i = g.n; i > 0; --i) {
+    g.dim[i] = g.dim[i - 1];
+    g.s0[i] = g.s0[i - 1];
+    g.s1[i] = g.s1[i - 1];
+  }
+  g.dim[0] = dim;
+  g.s0[0] = s0;
+  g.s1[0] = s1;
+  g.n++;
+  return true;
+}
+
+void Program::batch(int nbt) {
+  if (nbt < 1) throw std::runtime_error("batch: trajectory count must be >= 1");
+  for (auto& op : ops)
+    if (op.kind == OP_PACK || op.kind == OP_TCGEMM)
+      throw std::runtime_error("batch: must run before the backend selection");
+  nb = nbt;
+  for (auto& sl : slots) sl.numel1 = sl.numel;
+  if (nb == 1) return;
+  // slots that depend on a per-trajectory input
+  std::vector<char> bt(slots.size(), 0);
+  for (int sl : {S_F, S_T1, S_T2, S_L1, S_L2, S_OUT, S_RES}) bt[sl] = 1;
+  bool changed = true;
+  while (changed) {
+    changed = false;
+    for (const auto& op : ops) {
+      bool any = false;
+      for (int r : op.reads)
+        if (r >= 0 && bt[r]) any = true;
+      if (any && op.write >= 0 && !bt[op.write]) {
+        bt[op.write] = 1;
+        changed = true;
+      }
+    }
+  }
+  for (size_t i = 0; i < slots.size(); ++i) {
+    slots[i].batched = bt[i] != 0;
+    if (bt[i]) slots[i].numel = slots[i].numel1 * nb;
+  }
+  for (auto& op : ops) {
+    if (op.kind == OP_GEMM) {
+      GemmArgs& g = op.g;
+      const bool ea = bt[op.sa], eb = bt[op.sb], ec = bt[op.sc];
+      if (!ec) {
+        if (ea || eb) throw std::runtime_error("batch: per-trajectory input into a shared output: " + op.tag);
+        continue;
+      }
+      const long long M1 = g.M, N1 = g.N, K = g.K;
+      const long long sa = bstride(op.sa), sb = bstride(op.sb), sc = bstride(op.sc);
+      const long long kMax = (1LL << 31) - 1;
+      const bool fold_m = ea && !eb && g.gm.n < kMaxModes && M1 * nb <= kMax;
+      const bool fold_n = !fold_m && !ea && eb && g.gn.n < kMaxModes && N1 * nb <= kMax;
+      if (fold_m) {
+        prepend_mode(g.gm, nb, sa, sc);  // one GEMM over all trajectories' rows
+        g.M = (int)(M1 * nb);
+      } else if (fold_n) {
+        prepend_mode(g.gn, nb, sb, sc);
+        g.N = (int)(N1 * nb);
+      } else {
+        g.nb = nb;
+        g.bsA = sa;
+        g.bsB = sb;
+        g.bsC = sc;
+      }
+      op.flops *= nb;
+      auto esz = [](int dt) { return dt == C64 ? 16LL : 8LL; };
+      op.bytes = (ea ? nb : 1) * M1 * K * esz(op.dta) + (eb ? nb : 1) * K * N1 * esz(op.dtb) +
+                 nb * M1 * N1 * esz(op.dtc) * (g.acc ? 2 : 1);
+      plan_gemm(op, op.zeroed);
+    } else if (op.kind == OP_ADD) {
+      AddArgs& a = op.a;
+      if (!bt[op.add_sc]) {
+        for (int t = 0; t < a.nt; ++t)
+          if (bt[op.add_slots[t][0]] || (op.add_slots[t][1] >= 0 && bt[op.add_slots[t][1]]))
+            throw std::runtime_error("batch: per-trajectory term into a shared output: " + op.tag);
+        continue;
+      }
+      if (a.nd >= kAddDims) throw std::runtime_error("batch: too many dimensions: " + op.tag);
+      for (int i = a.nd; i > 0; --i) {
+        a.d[i] = a.d[i - 1];
+        a.sC[i] = a.sC[i - 1];
+        for (int t = 0; t < a.nt; ++t) {
+          a.t[t].sA[i] = a.t[t].sA[i - 1];
+          a.t[t].sB[i] = a.t[t].sB[i - 1];
+        }
+      }
+      a.d[0] = nb;
+      a.sC[0] = bstride(op.add_sc);
+      for (int t = 0; t < a.nt; ++t) {
+        a.t[t].sA[0] = bstride(op.add_slots[t][0]);
+        a.t[t].sB[0] = op.add_slots[t][1] >= 0 ? bstride(op.add_slots[t][1]) : 0;
+      }
+      a.nd++;
+      a.total *= nb;
+      op.bytes *= nb;
+      coalesce(a);
+    } else if (op.kind == OP_TRACE) {
+      op.tr_nb = nb;
+      for (int k = 0; k < 4; ++k) op.tr_bs[k] = bstride(op.tr_slots[k]);
+      op.tr_bsres = bstride(S_RES);
+    }
+  }
+}
+
 long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned) {
   long long bytes = 0;
   if (bases.size() < slots.size()) bases.resize(slots.size(), nullptr);
@@ -463,7 +634,7 @@ cudaError_t Program::launch_op(const Op& op, const std::vector<void*>& bases, cu
   } else if (op.kind == OP_TRACE) {
     e = launch_trace(dims.n, dims.o, op.tr_n_mu, static_cast<const double*>(bases[S_MU]),
                      bases[op.tr_slots[0]], bases[op.tr_slots[1]], bases[op.tr_slots[2]],
-                     bases[op.tr_slots[3]], bases[S_RES], st);
+                     bases[op.tr_slots[3]], bases[S_RES], op.tr_nb, op.tr_bs, op.tr_bsres, st);
   } else if (op.kind == OP_PACK) {
     PackArgs p = op.pk;
     p.src = at(bases, op.pk_src, op.pk_off, op.pk_dt);
@@ -636,7 +807,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
       continue;
     }
     const long long M = op.g.M, N = op.g.N, K = op.g.K;
-    if (M * N * K < min_macs || K < min_k) {
+    if (M * N * K * std::max(op.g.nb, 1) < min_macs || K < min_k) {
       push_op(op);
       continue;
     }
@@ -648,6 +819,9 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     }
     const bool ac = op.dta == C64, bc = op.dtb == C64;
     const long long rA = rup(M * (ac ? 2 : 1), BM), rB = rup(N * (bc ? 2 : 1), BN), Kp = rup(K, BK);
+    // batched products: an operand with a batch stride is packed per batch
+    const int nbt = std::max(op.g.nb, 1);
+    const int nbA = (nbt > 1 && op.g.bsA != 0) ? nbt : 1, nbB = (nbt > 1 && op.g.bsB != 0) ? nbt : 1;
     auto packed_slot = [&](const std::string& nm, long long rows, long long& exp_off) {
       exp_off = rup((long long)S * rows * Kp * 2, 256);
       int d1[1] = {(int)0};
@@ -674,12 +848,14 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     pa.pk.rows_pad = (int)rA;
     pa.pk.K_pad = (int)Kp;
     pa.pk.S = S;
+    pa.pk.nb = nbA;
+    pa.pk.bs = op.g.bsA;
     pa.pk_src = op.sa;
     pa.pk_off = op.oa;
     pa.pk_dt = op.dta;
     pa.reads = {op.sa};
     pa.write = pa.pk_dst;
-    pa.bytes = M * K * elem_bytes(op.dta) + (long long)S * rA * Kp * 2;
+    pa.bytes = nbA * (M * K * elem_bytes(op.dta) + (long long)S * rA * Kp * 2);
     // B: rows = N modes (strides g.gn.s0), K modes strides g.gk.s1
     pb.pk = PackArgs{};
     pb.pk.cplx = bc;
@@ -691,11 +867,13 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     pb.pk.rows_pad = (int)rB;
     pb.pk.K_pad = (int)Kp;
     pb.pk.S = S;
+    pb.pk.nb = nbB;
+    pb.pk.bs = op.g.bsB;
     pb.pk_src = op.sb;
     pb.pk_off = op.ob;
     pb.pk_dt = op.dtb;
     pb.reads = {op.sb};
-    pb.bytes = N * K * elem_bytes(op.dtb) + (long long)S * rB * Kp * 2;
+    pb.bytes = nbB * (N * K * elem_bytes(op.dtb) + (long long)S * rB * Kp * 2);
     // resolve packed slots (reuse an identical, still valid packing)
     bool emit_a = true, emit_b = true;
     auto resolve = [&](Op& pk, const ModeGroup& gr, const ModeGroup& gk, bool k_s1, long long rows,
@@ -703,7 +881,8 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
       const std::string key = std::to_string(pk.pk_src) + "@" + std::to_string(pk.pk_off) + "#" +
                               std::to_string(pk.pk_dt) + "|" + group_key(gr, false) + "|" +
                               group_key(gk, k_s1) + "|" + std::to_string(rows) + "x" + std::to_string(Kp) +
-                              "s" + std::to_string(S);
+                              "s" + std::to_string(S) + "b" + std::to_string(pk.pk.nb) + ":" +
+                              std::to_string(pk.pk.bs);
       auto it = pack_cache.find(key);
       if (it != pack_cache.end() && last_write[it->second.src] < (long long)it->second.pos) {
         pk.pk_dst = it->second.slot;
@@ -711,7 +890,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
         emit = false;
         return;
       }
-      pk.pk_dst = packed_slot(nm, rows, pk.pk_exp_off);
+      pk.pk_dst = packed_slot(nm, rows * pk.pk.nb, pk.pk_exp_off);
       pk.write = pk.pk_dst;
       emit = true;
       pack_cache[key] = PackRef{pk.pk_dst, pk.pk_exp_off, (size_t)-1, pk.pk_src};
@@ -737,6 +916,10 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     a.N = (int)N;
     a.rowsA_pad = (int)rA;
     a.rowsB_pad = (int)rB;
+    a.nb = nbt;
+    a.bat_a = nbA > 1;
+    a.bat_b = nbB > 1;
+    a.bsC = op.g.bsC;
     a.kblocks = (int)(Kp / BK);
     a.S = S;
     int cols = 32;
@@ -756,7 +939,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     a.acc = op.g.acc;
     // split K so that few output tiles still occupy the SMs: one CTA per SM,
     // cost = waves x (K blocks per CTA + fixed pipeline/epilogue overhead)
-    const long long ctas = (rB / BN) * (rA / BM);
+    const long long ctas = (rB / BN) * (rA / BM) * nbt;
     long long splits = 1;
     {
       double best = 1e300;
@@ -773,8 +956,9 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     }
     a.kb_per_split = (int)((a.kblocks + splits - 1) / splits);
     splits = (a.kblocks + a.kb_per_split - 1) / a.kb_per_split;
+    a.nsplit = (int)splits;
     a.atomic = splits > 1 ? 1 : 0;
-    t.bytes = (long long)S * (rA + rB) * Kp * 2 + M * N * elem_bytes(op.dtc);
+    t.bytes = (long long)S * (nbA * rA + nbB * rB) * Kp * 2 + nbt * M * N * elem_bytes(op.dtc);
     t.reads = {pa.pk_dst, pb.pk_dst};
     if (a.acc || a.atomic) t.reads.push_back(op.sc);
     t.write = op.sc;
@@ -791,30 +975,36 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
       z.tag = op.tag + ":zero";
       AddArgs& za = z.a;
       memset(&za, 0, sizeof(za));
-      int nd = 0;
-      long long dims[6], strd[6];
-      for (int i = 0; i < op.g.gm.n; ++i, ++nd) {
-        dims[nd] = op.g.gm.dim[i];
-        strd[nd] = op.g.gm.s1[i];
+      // output modes: batch, then the M and N groups (strides s1), sorted by
+      // decreasing stride so that the coalescing can merge them
+      std::vector<std::pair<long long, int>> md;
+      if (nbt > 1) md.push_back({op.g.bsC, nbt});
+      for (int i = 0; i < op.g.gm.n; ++i) md.push_back({op.g.gm.s1[i], op.g.gm.dim[i]});
+      for (int i = 0; i < op.g.gn.n; ++i) md.push_back({op.g.gn.s1[i], op.g.gn.dim[i]});
+      std::stable_sort(md.begin(), md.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+      std::vector<std::pair<long long, int>> mm;
+      for (const auto& x : md) {
+        if (!mm.empty() && mm.back().first == x.first * x.second) {
+          mm.back().first = x.first;
+          mm.back().second *= x.second;
+        } else if (x.second > 1) {
+          mm.push_back(x);
+        }
       }
-      for (int i = 0; i < op.g.gn.n; ++i, ++nd) {
-        dims[nd] = op.g.gn.dim[i];
-        strd[nd] = op.g.gn.s1[i];
+      if ((int)mm.size() > kAddDims) throw std::runtime_error("tensor-core output with too many modes: " + op.tag);
+      za.nd = std::max<int>(1, (int)mm.size());
+      for (int i = 0; i < kAddDims; ++i) {
+        za.d[i] = i < (int)mm.size() ? mm[i].second : 1;
+        za.sC[i] = i < (int)mm.size() ? mm[i].first : 0;
       }
-      if (nd > 4) throw std::runtime_error("tensor-core output with more than 4 modes: " + op.tag);
-      for (int i = 0; i < 4; ++i) {
-        const int k = i - (4 - nd);
-        za.d[i] = k >= 0 ? (int)dims[k] : 1;
-        za.sC[i] = k >= 0 ? strd[k] : 0;
-      }
-      za.total = M * N;
+      za.total = M * N * nbt;
       za.cc = op.dtc == C64;
       za.acc = 0;
       za.nt = 0;
       z.add_sc = op.sc;
       z.add_oc = op.oc;
       z.write = op.sc;
-      z.bytes = M * N * elem_bytes(op.dtc);
+      z.bytes = nbt * M * N * elem_bytes(op.dtc);
       push_op(z);
     }
     push_op(t);

@@ -29,27 +29,35 @@ __device__ double2 field_value(const tdcc_field& f, double t) {
   }
 }
 
-// ctx->t += dt (the reference advances t before the stages), then the field
-// at t, t + dt/2, t + dt.
+// ctx->t += dt (the reference advances t before the stages), then each
+// trajectory's field at t, t + dt/2, t + dt.  One block: every thread reads
+// the old time before thread 0 stores the new one.
 __global__ void advance_field_kernel(StepCtx* ctx) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    const double t = __dadd_rn(ctx->t, ctx->dt);
-    ctx->t = t;
-    const double h = ctx->dt / 2.0;
-    ctx->E[0] = field_value(ctx->field, t);
-    ctx->E[1] = field_value(ctx->field, __dadd_rn(t, h));
-    ctx->E[2] = field_value(ctx->field, __dadd_rn(t, ctx->dt));
+  const double t = __dadd_rn(ctx->t, ctx->dt);
+  const double dt = ctx->dt, h = dt / 2.0;
+  const int b = threadIdx.x;
+  if (b < ctx->nb) {
+    const tdcc_field& f = ctx->fields[b];
+    double2* E = ctx->E + 3 * b;
+    E[0] = field_value(f, t);
+    E[1] = field_value(f, __dadd_rn(t, h));
+    E[2] = field_value(f, __dadd_rn(t, dt));
   }
+  __syncthreads();
+  if (threadIdx.x == 0) ctx->t = t;
 }
 
-// Fs[s] = fock - E[s] * mu_z  for the three stage times
+// Fs[s][b] = fock - E[b][s] * mu[pol[b]]  for the three stage times
 __global__ void dress_kernel(const StepCtx* ctx, const double* __restrict__ fock,
-                             const double* __restrict__ muz, double2* __restrict__ Fs, int nn) {
-  const int s = blockIdx.y;
-  const double2 E = ctx->E[s];
+                             const double* __restrict__ mu, double2* __restrict__ Fs, int nn) {
+  const int s = blockIdx.y, b = blockIdx.z;
+  const int nb = ctx->nb;
+  const double2 E = ctx->E[3 * b + s];
+  const double* m = mu + (long long)ctx->pol[b] * nn;
+  double2* out = Fs + ((long long)s * nb + b) * nn;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += gridDim.x * blockDim.x) {
-    const double m = muz[e];
-    Fs[(long long)s * nn + e] = make_double2(fock[e] - E.x * m, -(E.y * m));
+    const double me = m[e];
+    out[e] = make_double2(fock[e] - E.x * me, -(E.y * me));
   }
 }
 
@@ -111,11 +119,14 @@ __global__ void rk4_finish_kernel(const double2* __restrict__ y0, const double2*
   }
 }
 
-__global__ void record_mu_kernel(StepCtx* ctx, const double2* res, int n_mu, double2* traj,
-                                 double* times) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    const long long s = ctx->step;
-    if (traj) traj[s] = res[n_mu - 1];
+__global__ void record_mu_kernel(StepCtx* ctx, const double2* res, double2* traj, double* times) {
+  const long long s = ctx->step;
+  const int nb = ctx->nb, b = threadIdx.x;
+  if (b < nb) {
+    if (traj) traj[s * nb + b] = res[(long long)b * ctx->n_mu + ctx->pol[b]];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
     if (times) times[s] = ctx->t;
     ctx->step = s + 1;
   }
@@ -128,17 +139,20 @@ static unsigned grid_for(long long n) {
   return (unsigned)b;
 }
 
-cudaError_t launch_advance_field(StepCtx* ctx, cudaStream_t st) {
-  advance_field_kernel<<<1, 32, 0, st>>>(ctx);
+static unsigned warps_for(int nb) { return (unsigned)((nb + 31) / 32 * 32); }
+
+cudaError_t launch_advance_field(StepCtx* ctx, int nb, cudaStream_t st) {
+  if (nb < 1 || nb > kMaxTrajectories) return cudaErrorInvalidValue;
+  advance_field_kernel<<<1, warps_for(nb), 0, st>>>(ctx);
   count_launch();
   return cudaGetLastError();
 }
 
-cudaError_t launch_dress(const StepCtx* ctx, const double* fock, const double* muz, double2* Fs,
-                         int n, cudaStream_t st) {
+cudaError_t launch_dress(const StepCtx* ctx, const double* fock, const double* mu, double2* Fs, int n,
+                         int nb, cudaStream_t st) {
   const int nn = n * n;
-  dim3 grid((nn + 255) / 256 > 64 ? 64 : (nn + 255) / 256, 3);
-  dress_kernel<<<grid, 256, 0, st>>>(ctx, fock, muz, Fs, nn);
+  dim3 grid((nn + 255) / 256 > 64 ? 64 : (nn + 255) / 256, 3, nb);
+  dress_kernel<<<grid, 256, 0, st>>>(ctx, fock, mu, Fs, nn);
   count_launch();
   return cudaGetLastError();
 }
@@ -157,9 +171,10 @@ cudaError_t launch_rk4_finish(const double2* y0, const double2* acc, double2* yn
   return cudaGetLastError();
 }
 
-cudaError_t launch_record_mu(StepCtx* ctx, const double2* res, int n_mu, double2* traj,
-                             double* times, cudaStream_t st) {
-  record_mu_kernel<<<1, 32, 0, st>>>(ctx, res, n_mu, traj, times);
+cudaError_t launch_record_mu(StepCtx* ctx, const double2* res, int nb, double2* traj, double* times,
+                             cudaStream_t st) {
+  if (nb < 1 || nb > kMaxTrajectories) return cudaErrorInvalidValue;
+  record_mu_kernel<<<1, warps_for(nb), 0, st>>>(ctx, res, traj, times);
   count_launch();
   return cudaGetLastError();
 }

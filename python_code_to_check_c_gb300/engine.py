@@ -53,9 +53,14 @@ def _stream():
 
 
 class CCEngine:
-    """One synthetic (or psi4-provided) system resident on the GPU."""
+    """One synthetic (or psi4-provided) system resident on the GPU.
 
-    def __init__(self, tei, fock, mu, o: int):
+    ``nb > 1`` advances nb trajectories over the same integrals together:
+    every per-trajectory array then carries a leading trajectory axis
+    (t1: (nb, o, v), t2: (nb, o, o, v, v), F: (nb, n, n)), dipoles are
+    (nb, n_mu) and propagated trajectories (nsteps, nb)."""
+
+    def __init__(self, tei, fock, mu, o: int, nb: int = 1):
         self.lib = _lib.load()
         self.tei = to_dev(tei, torch.float64)
         self.fock = to_dev(fock, torch.float64)
@@ -66,16 +71,34 @@ class CCEngine:
         self.v = self.n - self.o
         if tuple(self.tei.shape) != (self.n,) * 4:
             raise ValueError("tei must be (n,n,n,n)")
+        self.nb = int(nb)
+        self.n_mu = int(self.mu.shape[0])
         h = ctypes.c_void_p()
-        check(self.lib.tdcc_system_create(self.o, self.v, _ptr(self.tei), _ptr(self.fock),
-                                          _ptr(self.mu), int(self.mu.shape[0]), ctypes.byref(h)),
-              "tdcc_system_create")
+        check(self.lib.tdcc_system_create_batched(self.o, self.v, _ptr(self.tei), _ptr(self.fock),
+                                                  _ptr(self.mu), self.n_mu, self.nb, ctypes.byref(h)),
+              "tdcc_system_create_batched")
         self.handle = h
         self.precision = "fp64"
 
     @classmethod
-    def from_system(cls, sysm):
-        return cls(sysm.tei(), sysm.fock, sysm.mu, sysm.o)
+    def from_system(cls, sysm, nb: int = 1):
+        return cls(sysm.tei(), sysm.fock, sysm.mu, sysm.o, nb=nb)
+
+    def set_fields(self, fields, pol=None):
+        """Per-trajectory fields (a list of nb ``make_field`` results) and the
+        dipole component each couples to (default: the last); None clears."""
+        if fields is None:
+            check(self.lib.tdcc_set_fields(self.handle, None, None), "tdcc_set_fields")
+            return
+        if len(fields) != self.nb:
+            raise ValueError(f"need {self.nb} fields")
+        arr = (_lib.TdccField * self.nb)(*fields)
+        parr = None
+        if pol is not None:
+            if len(pol) != self.nb:
+                raise ValueError(f"need {self.nb} polarisations")
+            parr = (ctypes.c_int * self.nb)(*[int(p) for p in pol])
+        check(self.lib.tdcc_set_fields(self.handle, arr, parr), "tdcc_set_fields")
 
     def close(self):
         if getattr(self, "handle", None):
@@ -113,7 +136,9 @@ class CCEngine:
         t2 = to_dev(t2)
         l1 = to_dev(l1) if l1 is not None else None
         l2 = to_dev(l2) if l2 is not None else None
-        F = to_dev(self.fock if F is None else F)
+        if F is None:
+            F = self.fock if self.nb == 1 else self.fock.expand(self.nb, self.n, self.n)
+        F = to_dev(F)
         out = torch.empty_like(t1 if block in (TDCC_T1, TDCC_L1) else t2)
         check(self.lib.tdcc_rhs(self.handle, m, block, _ptr(t1), _ptr(t2), _ptr(l1), _ptr(l2),
                                 _ptr(F), _ptr(out), _stream()), "tdcc_rhs")
@@ -177,10 +202,10 @@ class CCEngine:
     # ---- density / dipole ----
     def dipole_moment(self, t1, t2, l1, l2, F=None):
         t1, t2, l1, l2 = (to_dev(x) for x in (t1, t2, l1, l2))
-        out = torch.empty(int(self.mu.shape[0]), dtype=torch.complex128, device=t1.device)
+        out = torch.empty(self.nb * self.n_mu, dtype=torch.complex128, device=t1.device)
         check(self.lib.tdcc_dipole(self.handle, _ptr(t1), _ptr(t2), _ptr(l1), _ptr(l2), _ptr(out),
                                    _stream()), "tdcc_dipole")
-        return out
+        return out if self.nb == 1 else out.view(self.nb, self.n_mu)
 
     # ---- propagation ----
     def rk4_step(self, method: str, state, t_prev: float, dt: float, field, precs: int = 15,
@@ -188,23 +213,30 @@ class CCEngine:
         """One reference loop-body step; returns (new_state, mu or None)."""
         t1, t2, l1, l2 = (to_dev(x) for x in state)
         outs = [torch.empty_like(x) for x in (t1, t2, l1, l2)]
-        mu = torch.empty(int(self.mu.shape[0]), dtype=torch.complex128, device=t1.device) if with_mu else None
+        mu = torch.empty(self.nb * self.n_mu, dtype=torch.complex128, device=t1.device) if with_mu else None
         check(self.lib.tdcc_rk4_step(self.handle, _lib.METHODS[method], _ptr(t1), _ptr(t2), _ptr(l1),
                                      _ptr(l2), *(_ptr(x) for x in outs), float(t_prev), float(dt),
-                                     int(precs), ctypes.byref(field), _ptr(mu), _stream()),
+                                     int(precs), ctypes.byref(field) if field is not None else None,
+                                     _ptr(mu), _stream()),
               "tdcc_rk4_step")
+        if mu is not None and self.nb > 1:
+            mu = mu.view(self.nb, self.n_mu)
         return tuple(outs), mu
 
     def propagate(self, method: str, state, t0: float, dt: float, nsteps: int, field, precs: int = 15):
         """nsteps device-resident steps (captured CUDA graph); returns
-        (final_state, mu_z trajectory as a complex128 CUDA tensor)."""
+        (final_state, mu_z trajectory as a complex128 CUDA tensor: (nsteps,),
+        or (nsteps, nb) for a batched engine).  field None: the fields of
+        ``set_fields``."""
         st = [to_dev(x).clone() for x in state]
-        traj = torch.empty(max(int(nsteps), 1), dtype=torch.complex128, device=st[0].device)
+        traj = torch.empty(max(int(nsteps), 1) * self.nb, dtype=torch.complex128, device=st[0].device)
         check(self.lib.tdcc_propagate(self.handle, _lib.METHODS[method], *(_ptr(x) for x in st),
                                       float(t0), float(dt), int(nsteps), int(precs),
-                                      ctypes.byref(field), _ptr(traj), _stream()),
+                                      ctypes.byref(field) if field is not None else None, _ptr(traj),
+                                      _stream()),
               "tdcc_propagate")
-        return tuple(st), traj[: int(nsteps)]
+        traj = traj[: int(nsteps) * self.nb]
+        return tuple(st), (traj if self.nb == 1 else traj.view(int(nsteps), self.nb))
 
 
 def profile_step(eng: "CCEngine", method: str, state, t_prev: float, dt: float, field, precs: int = 15):

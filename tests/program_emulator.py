@@ -51,20 +51,21 @@ class Emulator:
         A = self.bufs[op["sa"]]
         B = self.bufs[op["sb"]]
         C = self.bufs[op["sc"]]
-        Am = A[op["oa"] + am[:, None] + ak[None, :]]
-        Bm = B[op["ob"] + bk[:, None] + bn[None, :]]
-        val = complex(op["ar"], op["ai"]) * (Am @ Bm)
-        if C.dtype == np.float64:
-            val = val.real
-        idx = op["oc"] + cm[:, None] + cn[None, :]
-        if op["acc"] or op["atomic"]:
-            C[idx] += val
-        else:
-            C[idx] = val
+        for z in range(op.get("nb", 1)):
+            Am = A[op["oa"] + z * op.get("bsA", 0) + am[:, None] + ak[None, :]]
+            Bm = B[op["ob"] + z * op.get("bsB", 0) + bk[:, None] + bn[None, :]]
+            val = complex(op["ar"], op["ai"]) * (Am @ Bm)
+            if C.dtype == np.float64:
+                val = val.real
+            idx = op["oc"] + z * op.get("bsC", 0) + cm[:, None] + cn[None, :]
+            if op["acc"] or op["atomic"]:
+                C[idx] += val
+            else:
+                C[idx] = val
 
     def _add(self, op):
         d = op["d"]
-        I = np.indices(d).reshape(4, -1).astype(np.int64)
+        I = np.indices(d).reshape(len(d), -1).astype(np.int64)
         C = self.bufs[op["sc"]]
         offc = op["oc"] + (I * np.array(op["sC"], dtype=np.int64)[:, None]).sum(0)
         s = np.zeros(I.shape[1], dtype=np.complex128)
@@ -85,12 +86,14 @@ class Emulator:
     def _trace(self, op):
         o, v, n = self.o, self.v, self.n
         dij, l1, dai, dab = (self.bufs[k] for k in op["slots"])
-        rho = np.zeros((n, n), dtype=np.complex128)
-        rho[:o, :o] = dij[: o * o].reshape(o, o)
-        rho[:o, o:] = l1[: o * v].reshape(o, v)
-        rho[o:, :o] = dai[: v * o].reshape(v, o)
-        rho[o:, o:] = dab[: v * v].reshape(v, v)
         mu = self.bufs[S_MU]
         res = self.bufs[S_RES]
-        for k in range(op["n_mu"]):
-            res[k] = (mu[k * n * n:(k + 1) * n * n].reshape(n, n) * rho).sum()
+        bs = op.get("bs", [0, 0, 0, 0])
+        for z in range(op.get("nb", 1)):
+            rho = np.zeros((n, n), dtype=np.complex128)
+            rho[:o, :o] = dij[z * bs[0]:][: o * o].reshape(o, o)
+            rho[:o, o:] = l1[z * bs[1]:][: o * v].reshape(o, v)
+            rho[o:, :o] = dai[z * bs[2]:][: v * o].reshape(v, o)
+            rho[o:, o:] = dab[z * bs[3]:][: v * v].reshape(v, v)
+            for k in range(op["n_mu"]):
+                res[z * op.get("bsres", 0) + k] = (mu[k * n * n:(k + 1) * n * n].reshape(n, n) * rho).sum()
