@@ -146,6 +146,8 @@ struct TcArgs {
   ModeGroup gmC, gnC;       // output offsets: strides in s0
   void* C;
   double ar, ai;
+  int alpha_pow2;           // alpha = (-1)^alpha_neg 2^alpha_e exactly (folded into exponents)
+  int alpha_e, alpha_neg;
   int acc, atomic;
   int* err;
 };

@@ -102,10 +102,17 @@ __global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
     mim = max(mim, __shfl_xor_sync(0xffffffffu, mim, d));
   }
   if (lane == 0) {
-    // max = f 2^e with f in [0.5, 1): e = biased exponent - 1022
-    const int Ere = (int)(mre >> 52), Eim = (int)(mim >> 52);
-    if (mre != 0) atomicMax(&exps[p.cplx ? 2 * m : m], (Ere > 0 ? Ere - 1022 : -1022) + kExpBias);
-    if (p.cplx && mim != 0) atomicMax(&exps[2 * m + 1], (Eim > 0 ? Eim - 1022 : -1022) + kExpBias);
+    // max = f 2^e with f in [0.5, 1): e = biased exponent - 1022.  The real
+    // and imaginary rows of a complex row share one exponent (that of the
+    // larger part), so that the slice-product epilogue combines
+    // re*re - im*im and re*im + im*re exactly in integers.
+    const unsigned long long mx = max(mre, mim);
+    const int E = (int)(mx >> 52);
+    if (mx != 0) {
+      const int eb = (E > 0 ? E - 1022 : -1022) + kExpBias;
+      atomicMax(&exps[p.cplx ? 2 * m : m], eb);
+      if (p.cplx) atomicMax(&exps[2 * m + 1], eb);
+    }
   }
 }
 
@@ -218,6 +225,21 @@ __device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_
 __device__ __forceinline__ void umma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
+__device__ __forceinline__ void tmem_ld16u(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_st16u(uint32_t taddr, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
   asm volatile(
@@ -241,7 +263,36 @@ struct TcShared {
   uint64_t accfull, accempty, done;
   uint32_t tmem;
   volatile int abort;  // set by any role on an expired wait; polled by all
+  long long col_off[TC_BN];  // output offset of each logical column of the tile (-1: outside)
+  int col_exp[TC_BN];        // exponent of each packed column of B
 };
+
+// x * 2^E rounded to nearest (ties to even) from the integer's bits: no FP64
+// arithmetic on the normal-range path (GB300's FP64 pipe is narrow).
+__device__ __forceinline__ double scaled_i64_to_double(long long x, int E) {
+  if (x == 0) return 0.0;
+  const unsigned long long sgn = x < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned long long u = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+  int msb = 63 - __clzll((long long)u);
+  unsigned long long mant;
+  if (msb <= 52) {
+    mant = u << (52 - msb);
+  } else {
+    const int sh = msb - 52;
+    mant = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      ++mant;
+      if (mant >> 53) {
+        mant >>= 1;
+        ++msb;
+      }
+    }
+  }
+  const int be = msb + E + 1023;
+  if (be <= 0 || be >= 2047) return ldexp((double)x, E);  // subnormal / overflow: rare
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (mant & 0x000FFFFFFFFFFFFFull)));
+}
 
 __device__ __forceinline__ void fail(TcShared* sh, int* err, int code) {
   sh->abort = 1;
@@ -377,119 +428,176 @@ __global__ void __launch_bounds__(192, 1)
     // below 2^52 per chunk: int64 holds up to 2^11 chunks.  No FP64
     // arithmetic until the final conversion -- the FP64 pipe is narrow.
     const int u = 7 * ((S < 5 ? S : 5) + 1);
-    long long acc[TC_BN];
-#pragma unroll
-    for (int j = 0; j < TC_BN; ++j) acc[j] = 0;
+    {
+      // per-tile column data, shared by all rows: output offsets and B exponents
+      const int t = threadIdx.x - 64;  // 0..127
+      constexpr int ncl = BC ? TC_BN / 2 : TC_BN;
+      if (t < ncl) {
+        const int n = nt * ncl + t;
+        long long o = -1;
+        if (n < g.N) decomp_tc(g.gnC, n, o);
+        sh->col_off[t] = o;
+      }
+      if (t < TC_BN) sh->col_exp[t] = row_exp(g.expB[rowB0 + nt * TC_BN + t]);
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps
+    }
+    // Row data and the staging tile of this warp (final chunk): the operand
+    // ring is idle once the last accumulators are complete.
+    const int prow = mt * TC_BM + row;          // packed row of A (within the batch)
+    const int m = AC ? (prow >> 1) : prow;
+    const bool odd = AC && (lane & 1);
+    constexpr int ncol_log = BC ? TC_BN / 2 : TC_BN;  // logical output columns in this tile
+    constexpr int rows_out = AC ? 16 : 32;             // logical output rows of this warp
+    constexpr int RS = ncol_log + 1;                    // staging row stride (double2), padded
+    double2* stage = reinterpret_cast<double2*>(sm) + (size_t)q * (32 * RS);
+    const int lr = AC ? (lane >> 1) : lane;            // this lane's staging row
+    const uint32_t tl = (uint32_t)(q * 32) << 16;      // TMEM lane base of this warp
+    const uint32_t t64 = (uint32_t)(S * TC_BN);        // int64 partial sums: 2 words per column
+    bool ok = true;
     for (int c = 0; c < nchunks; ++c) {
-      // warp-uniform decisions: tcgen05.ld and the shuffles below are collective
-      if (__any_sync(0xffffffffu, sh->abort != 0)) break;
+      // warp-uniform decisions: tcgen05.ld/st and the shuffles below are collective
+      if (__any_sync(0xffffffffu, sh->abort != 0)) {
+        ok = false;
+        break;
+      }
       const bool got = mbar_wait(smem_u32(&sh->accfull), (uint32_t)(c & 1), kWaitLimit);
       if (!__all_sync(0xffffffffu, got)) {
         fail(sh, g.err, 4);
+        ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-#pragma unroll
+      const bool last = c == nchunks - 1;
+      int ebase = 0;
+      if (last) {
+        const int ea = prow < g.rowsA_pad ? row_exp(g.expA[rowA0 + prow]) : 0;
+        ebase = ea - u + (g.alpha_pow2 ? g.alpha_e : 0);
+      }
+      // 16 columns at a time (a runtime loop keeps the code small)
+#pragma unroll 1
       for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+        long long a16[16];
+        if (c == 0) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) a16[j] = 0;
+        } else {
+          uint32_t lo[16], hi[16];
+          tmem_ld16u(tmem + tl + t64 + 2 * j0, lo);
+          tmem_ld16u(tmem + tl + t64 + 2 * j0 + 16, hi);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) a16[j] = (long long)(((unsigned long long)hi[j] << 32) | lo[j]);
+        }
         for (int L = 2; L <= S + 1; ++L) {
           float v[16];
-          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((L - 2) * TC_BN + j0), v);
+          tmem_ld16(tmem + tl + (uint32_t)((L - 2) * TC_BN + j0), v);
           const int sh = u - 7 * L;
           // |v| <= 2^24: a 32-bit conversion is exact and stays off the FP64 pipe
           if (sh >= 0) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j0 + j] += (long long)__float2int_rn(v[j]) << sh;
+            for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(v[j]) << sh;
           } else {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j0 + j] += (long long)__float2int_rn(v[j]) >> (-sh);
+            for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(v[j]) >> (-sh);
           }
         }
+        if (!last) {
+          uint32_t lo[16], hi[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            lo[j] = (uint32_t)(unsigned long long)a16[j];
+            hi[j] = (uint32_t)((unsigned long long)a16[j] >> 32);
+          }
+          tmem_st16u(tmem + tl + t64 + 2 * j0, lo);
+          tmem_st16u(tmem + tl + t64 + 2 * j0 + 16, hi);
+          continue;
+        }
+        // final chunk: combine, scale back, stage (lanes own rows here)
+        const bool neg = g.alpha_pow2 && g.alpha_neg;
+        constexpr int NJ = BC ? 8 : 16;  // logical columns in this group
+#pragma unroll
+        for (int k = 0; k < NJ; ++k) {
+          const int jj = (BC ? j0 / 2 : j0) + k;
+          // integer combine: the pair exponents are shared, so these are exact
+          long long re, im;
+          if constexpr (BC) {
+            const long long x0 = a16[2 * k], x1 = a16[2 * k + 1];
+            if constexpr (AC) {
+              const long long p0 = __shfl_xor_sync(0xffffffffu, x0, 1);
+              const long long p1 = __shfl_xor_sync(0xffffffffu, x1, 1);
+              // even lane: (rr, ri) own, (ir, ii) partner; odd lane the reverse
+              const long long rr = odd ? p0 : x0, ri = odd ? p1 : x1, ir = odd ? x0 : p0, ii = odd ? x1 : p1;
+              re = rr - ii;
+              im = ri + ir;
+            } else {
+              re = x0;
+              im = x1;
+            }
+          } else {
+            const long long x = a16[k];
+            if constexpr (AC) {
+              const long long p = __shfl_xor_sync(0xffffffffu, x, 1);
+              re = odd ? p : x;
+              im = odd ? x : p;
+            } else {
+              re = x;
+              im = 0;
+            }
+          }
+          // with complex A the two lanes of a pair hold the same output: split columns
+          if (AC && ((jj & 1) != (lane & 1))) continue;
+          const int E = ebase + sh->col_exp[BC ? 2 * jj : jj];
+          double vr, vi;
+          if (g.alpha_pow2) {
+            vr = scaled_i64_to_double(neg ? -re : re, E);
+            vi = scaled_i64_to_double(neg ? -im : im, E);
+          } else {
+            const double dr = scaled_i64_to_double(re, E), di = scaled_i64_to_double(im, E);
+            vr = g.ar * dr - g.ai * di;
+            vi = g.ar * di + g.ai * dr;
+          }
+          stage[lr * RS + jj] = make_double2(vr, vi);
+        }
       }
+      if (!last) asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(smem_u32(&sh->accempty));
     }
-    if (!__any_sync(0xffffffffu, sh->abort != 0)) {
-      // scale back and write
-      const int prow = mt * TC_BM + row;          // packed row of A (within the batch)
-      const int ea = prow < g.rowsA_pad ? row_exp(g.expA[rowA0 + prow]) : 0;
-      // converted in place: acc[j] then holds the bits of the FP64 value
-#pragma unroll
-      for (int j = 0; j < TC_BN; ++j) {
-        const int pcol = nt * TC_BN + j;
-        const int E = ea + row_exp(g.expB[rowB0 + pcol]) - u;
-        // 2^E built from its bits (one multiply instead of ldexp)
-        const double s2 = (E > -1023 && E < 1024) ? __longlong_as_double((long long)(E + 1023) << 52)
-                                                  : ldexp(1.0, E);
-        acc[j] = __double_as_longlong((double)acc[j] * s2);
-      }
-      const int m = AC ? (prow >> 1) : prow;
-      const bool odd = AC && (lane & 1);
+    if (ok && !__any_sync(0xffffffffu, sh->abort != 0)) {
+      // write the staged tile: lanes own columns, so stores are contiguous
+      __syncwarp();
       long long coffm = 0;
       if (m < g.M) decomp_tc(g.gmC, m, coffm);
       double2* C = static_cast<double2*>(g.C) + (g.cc ? zb * g.bsC : 0);
-      constexpr int ncol_log = BC ? TC_BN / 2 : TC_BN;  // logical output columns in this tile
-#pragma unroll
-      for (int jj = 0; jj < ncol_log; ++jj) {
-        double re, im;
-        if constexpr (BC) {
-          const double x0 = __longlong_as_double(acc[2 * jj]), x1 = __longlong_as_double(acc[2 * jj + 1]);
-          if constexpr (AC) {
-            const double p0 = __shfl_xor_sync(0xffffffffu, x0, 1);
-            const double p1 = __shfl_xor_sync(0xffffffffu, x1, 1);
-            // even lane: (rr, ri) own, (ir, ii) partner; odd lane the reverse
-            const double rr = odd ? p0 : x0, ri = odd ? p1 : x1, ir = odd ? x0 : p0, ii = odd ? x1 : p1;
-            re = rr - ii;
-            im = ri + ir;
+      double* Cr = static_cast<double*>(g.C) + (g.cc ? 0 : zb * g.bsC);
+      const int m0w = AC ? ((mt * TC_BM + q * 32) >> 1) : (mt * TC_BM + q * 32);
+      for (int r = 0; r < rows_out; ++r) {
+        const long long cm = __shfl_sync(0xffffffffu, coffm, AC ? 2 * r : r);
+        if (m0w + r >= g.M) break;  // warp-uniform
+        for (int cc = lane; cc < ncol_log; cc += 32) {
+          const long long cn = sh->col_off[cc];
+          if (cn < 0) continue;
+          const long long off = cm + cn;
+          const double2 v = stage[r * RS + cc];
+          if (g.cc) {
+            if (g.atomic) {
+              atomicAdd(&C[off].x, v.x);
+              atomicAdd(&C[off].y, v.y);
+            } else if (g.acc) {
+              double2 cv = C[off];
+              cv.x += v.x;
+              cv.y += v.y;
+              C[off] = cv;
+            } else {
+              C[off] = v;
+            }
           } else {
-            re = x0;
-            im = x1;
+            if (g.atomic)
+              atomicAdd(&Cr[off], v.x);
+            else if (g.acc)
+              Cr[off] += v.x;
+            else
+              Cr[off] = v.x;
           }
-        } else {
-          const double x = __longlong_as_double(acc[jj]);
-          if constexpr (AC) {
-            const double p = __shfl_xor_sync(0xffffffffu, x, 1);
-            re = odd ? p : x;
-            im = odd ? x : p;
-          } else {
-            re = x;
-            im = 0.0;
-          }
-        }
-        // with complex A the two lanes of a pair hold the same output: split columns
-        if (AC && ((jj & 1) != (lane & 1))) continue;
-        const int n = nt * ncol_log + jj;
-        if (m >= g.M || n >= g.N) continue;
-        long long coffn;
-        decomp_tc(g.gnC, n, coffn);
-        const long long off = coffm + coffn;
-        double vr, vi;
-        if (g.ai == 0.0) {  // the equations' coefficients are real
-          vr = g.ar * re;
-          vi = g.ar * im;
-        } else {
-          vr = g.ar * re - g.ai * im;
-          vi = g.ar * im + g.ai * re;
-        }
-        if (g.cc) {
-          if (g.atomic) {
-            atomicAdd(&C[off].x, vr);
-            atomicAdd(&C[off].y, vi);
-          } else if (g.acc) {
-            double2 cv = C[off];
-            cv.x += vr;
-            cv.y += vi;
-            C[off] = cv;
-          } else {
-            C[off] = make_double2(vr, vi);
-          }
-        } else {
-          double* Cr = static_cast<double*>(g.C) + zb * g.bsC;
-          if (g.atomic)
-            atomicAdd(&Cr[off], vr);
-          else if (g.acc)
-            Cr[off] += vr;
-          else
-            Cr[off] = vr;
         }
       }
     }

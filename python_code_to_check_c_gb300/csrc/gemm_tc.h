@@ -15,7 +15,7 @@ constexpr int TC_STAGES = 8;                 // shared-memory ring depth
 constexpr int TC_CHUNK_KB = 16;              // 1024-wide K chunks (exact FP32 sums)
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
-constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 256;
+constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 2048;
 constexpr int TC_MAX_SLICES = 7;
 
 }  // namespace tdcc

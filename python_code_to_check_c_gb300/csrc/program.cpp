@@ -4,6 +4,7 @@
 // (ops independent of the RK4 block's varying inputs, run once per step)
 // and the per-stage body.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -923,7 +924,8 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     a.kblocks = (int)(Kp / BK);
     a.S = S;
     int cols = 32;
-    while (cols < S * BN) cols *= 2;
+    while (cols < (S + 2) * BN) cols *= 2;  // S level accumulators + int64 partial sums
+    if (cols > 512) throw std::runtime_error("tensor-core tile needs more than 512 TMEM columns");
     a.tmem_cols = cols;
     a.ac = ac;
     a.bc = bc;
@@ -936,6 +938,15 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     }
     a.ar = op.g.ar;
     a.ai = op.g.ai;
+    {
+      // real power-of-two coefficients (the equations' +-1, +-1/2, +-1/4 ...)
+      // are applied exactly in the exponent of the epilogue's conversion
+      int e2 = 0;
+      const double fr = std::frexp(std::fabs(op.g.ar), &e2);
+      a.alpha_pow2 = (op.g.ai == 0.0 && op.g.ar != 0.0 && fr == 0.5) ? 1 : 0;
+      a.alpha_e = e2 - 1;
+      a.alpha_neg = op.g.ar < 0.0 ? 1 : 0;
+    }
     a.acc = op.g.acc;
     // split K so that few output tiles still occupy the SMs: one CTA per SM,
     // cost = waves x (K blocks per CTA + fixed pipeline/epilogue overhead)
