@@ -19,9 +19,11 @@
 // operands are combined with a lane-pair shuffle and written through the
 // same strided output decoder as the FP64 kernel.
 //
-// Pipeline: 6 warps.  Warp 0 issues TMA loads (SWIZZLE_128B) into an
-// 8-stage shared-memory ring, one (A_s, B_s) slice pair per stage; warp 1
-// owns TMEM and issues the MMAs from one thread; warps 2-5 drain TMEM.
+// Pipeline: 2 + TC_EPI_WARPS warps.  Warp 0 issues TMA loads
+// (SWIZZLE_128B) into an 8-stage shared-memory ring, one (A_s, B_s) slice
+// pair per stage; warp 1 owns TMEM and issues the MMAs from one thread; the
+// other warps drain TMEM, TC_EPI_WARPS / 4 per TMEM lane quarter, each
+// taking a slice of the tile's columns.
 // Every wait has an iteration limit: on expiry the kernel records an error
 // code, stops issuing work, waits (bounded) for its own operations and frees
 // TMEM before returning.
@@ -233,6 +235,15 @@ __device__ __forceinline__ void tmem_ld16u(uint32_t taddr, uint32_t* r) {
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 }
+// issue only: the caller waits (tcgen05.wait::ld) before reading r
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
 __device__ __forceinline__ void tmem_st16u(uint32_t taddr, const uint32_t* r) {
   asm volatile(
       "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
@@ -300,7 +311,7 @@ __device__ __forceinline__ void fail(TcShared* sh, int* err, int code) {
 }
 
 template <bool AC, bool BC>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(TC_THREADS, 1)
     ozaki_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs g) {
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -317,7 +328,7 @@ __global__ void __launch_bounds__(192, 1)
       mbar_init(smem_u32(&sh->empty[i]), 1);
     }
     mbar_init(smem_u32(&sh->accfull), 1);
-    mbar_init(smem_u32(&sh->accempty), 128);
+    mbar_init(smem_u32(&sh->accempty), 32 * TC_EPI_WARPS);
     mbar_init(smem_u32(&sh->done), 1);
     sh->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -418,8 +429,14 @@ __global__ void __launch_bounds__(192, 1)
       mbar_wait(smem_u32(&sh->done), 0, kWaitLimit);
     }
   } else {
-    // ---------------- epilogue (warps 2..5) ----------------
+    // ---------------- epilogue (warps 2 .. 2 + TC_EPI_WARPS - 1) ----------------
+    // TC_EPI_WARPS / 4 warps per TMEM lane quarter, each owning a slice of the
+    // tile's columns: the drain is latency-bound per warp, so the work is
+    // spread over warps.
+    constexpr int kWq = TC_EPI_WARPS / 4;   // warps per lane quarter
+    constexpr int kCw = TC_BN / kWq;        // packed columns per warp (multiple of 16)
     const int q = warp & 3;             // TMEM lane quarter this warp may access
+    const int hcol = (warp - 2) >> 2;   // column slice of this warp
     const int row = q * 32 + lane;      // tile row == TMEM lane
     // Exact sums in integer units of 2^-u, u = 7 (min(S,5) + 1).  The level
     // sums are integers (products of integer slices, FP32-exact per chunk),
@@ -430,7 +447,7 @@ __global__ void __launch_bounds__(192, 1)
     const int u = 7 * ((S < 5 ? S : 5) + 1);
     {
       // per-tile column data, shared by all rows: output offsets and B exponents
-      const int t = threadIdx.x - 64;  // 0..127
+      const int t = threadIdx.x - 64;  // 0 .. 32 * TC_EPI_WARPS - 1
       constexpr int ncl = BC ? TC_BN / 2 : TC_BN;
       if (t < ncl) {
         const int n = nt * ncl + t;
@@ -439,7 +456,7 @@ __global__ void __launch_bounds__(192, 1)
         sh->col_off[t] = o;
       }
       if (t < TC_BN) sh->col_exp[t] = row_exp(g.expB[rowB0 + nt * TC_BN + t]);
-      asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI_WARPS) : "memory");  // the epilogue warps
     }
     // Row data and the staging tile of this warp (final chunk): the operand
     // ring is idle once the last accumulators are complete.
@@ -475,29 +492,43 @@ __global__ void __launch_bounds__(192, 1)
       }
       // 16 columns at a time (a runtime loop keeps the code small)
 #pragma unroll 1
-      for (int j0 = 0; j0 < TC_BN; j0 += 16) {
+      for (int j0 = hcol * kCw; j0 < (hcol + 1) * kCw; j0 += 16) {
+        // all loads of the group in flight before one wait (TMEM latency)
+        constexpr int kMaxLv = 6;  // levels 2..7 (S <= 6)
         long long a16[16];
-        if (c == 0) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) a16[j] = 0;
-        } else {
+        if (c > 0) {
           uint32_t lo[16], hi[16];
-          tmem_ld16u(tmem + tl + t64 + 2 * j0, lo);
-          tmem_ld16u(tmem + tl + t64 + 2 * j0 + 16, hi);
+          tmem_ld16_nowait(tmem + tl + t64 + 2 * j0, lo);
+          tmem_ld16_nowait(tmem + tl + t64 + 2 * j0 + 16, hi);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
           for (int j = 0; j < 16; ++j) a16[j] = (long long)(((unsigned long long)hi[j] << 32) | lo[j]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) a16[j] = 0;
         }
-        for (int L = 2; L <= S + 1; ++L) {
-          float v[16];
-          tmem_ld16(tmem + tl + (uint32_t)((L - 2) * TC_BN + j0), v);
-          const int sh = u - 7 * L;
-          // |v| <= 2^24: a 32-bit conversion is exact and stays off the FP64 pipe
-          if (sh >= 0) {
+        // levels in batches of three loads before one wait
 #pragma unroll
-            for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(v[j]) << sh;
-          } else {
+        for (int L0 = 2; L0 <= kMaxLv + 1; L0 += 3) {
+          if (L0 > S + 1) break;
+          uint32_t lv[3][16];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(v[j]) >> (-sh);
+          for (int i = 0; i < 3; ++i)
+            if (L0 + i <= S + 1) tmem_ld16_nowait(tmem + tl + (uint32_t)((L0 + i - 2) * TC_BN + j0), lv[i]);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const int L = L0 + i;
+            if (L > S + 1) break;
+            const int sh = u - 7 * L;
+            // |v| <= 2^24: a 32-bit conversion is exact and stays off the FP64 pipe
+            if (sh >= 0) {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(__uint_as_float(lv[i][j])) << sh;
+            } else {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(__uint_as_float(lv[i][j])) >> (-sh);
+            }
           }
         }
         if (!last) {
@@ -570,11 +601,15 @@ __global__ void __launch_bounds__(192, 1)
       double2* C = static_cast<double2*>(g.C) + (g.cc ? zb * g.bsC : 0);
       double* Cr = static_cast<double*>(g.C) + (g.cc ? 0 : zb * g.bsC);
       const int m0w = AC ? ((mt * TC_BM + q * 32) >> 1) : (mt * TC_BM + q * 32);
-      for (int r = 0; r < rows_out; ++r) {
+      constexpr int NCW = ncol_log / kWq;  // logical columns of this warp (<= 32)
+      const int cc = hcol * NCW + lane;   // this lane's column while storing
+      const long long cn_l = lane < NCW ? sh->col_off[cc] : -1;
+      const int nrows = min(rows_out, g.M - m0w);
+#pragma unroll 4
+      for (int r = 0; r < nrows; ++r) {
         const long long cm = __shfl_sync(0xffffffffu, coffm, AC ? 2 * r : r);
-        if (m0w + r >= g.M) break;  // warp-uniform
-        for (int cc = lane; cc < ncol_log; cc += 32) {
-          const long long cn = sh->col_off[cc];
+        {
+          const long long cn = cn_l;
           if (cn < 0) continue;
           const long long off = cm + cn;
           const double2 v = stage[r * RS + cc];
@@ -691,13 +726,13 @@ cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, 
   const CUtensorMap mb = slice_map(packB, a.S, (a.bat_b ? a.nb : 1) * a.rowsB_pad, a.kblocks * TC_BK, TC_BN);
   dim3 grid(a.rowsB_pad / TC_BN, a.rowsA_pad / TC_BM, (unsigned)((long long)a.nb * a.nsplit));
   if (a.ac && a.bc)
-    ozaki_kernel<true, true><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<true, true><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
   else if (a.ac)
-    ozaki_kernel<true, false><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<true, false><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
   else if (a.bc)
-    ozaki_kernel<false, true><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<false, true><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
   else
-    ozaki_kernel<false, false><<<grid, 192, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<false, false><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
   count_launch();
   return cudaGetLastError();
 }

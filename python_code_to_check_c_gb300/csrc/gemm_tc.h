@@ -16,6 +16,8 @@ constexpr int TC_CHUNK_KB = 16;              // 1024-wide K chunks (exact FP32 s
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
 constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 2048;
-constexpr int TC_MAX_SLICES = 7;
+constexpr int TC_MAX_SLICES = 6;
+constexpr int TC_EPI_WARPS = 16;             // TMEM drain warps (four per lane quarter)
+constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;  // + TMA producer warp + MMA warp
 
 }  // namespace tdcc

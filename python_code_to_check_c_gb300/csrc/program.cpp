@@ -775,7 +775,7 @@ static long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
 
 void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k) {
   if (prec_mode != 1) return;
-  if (S < 1 || S > 7) throw std::runtime_error("slices must be 1..7");
+  if (S < 1 || S > 6) throw std::runtime_error("slices must be 1..6");
   constexpr int BM = 128, BN = 64, BK = 64;  // tensor-core tile (gemm_tc.h)
   std::vector<Op> out;
   out.reserve(ops.size() * 2);
