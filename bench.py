@@ -1,16 +1,26 @@
 """Benchmark: TD-CCSD RK4 steps/s on one GB300 (replicas across GPUs).
 
-One "step" is the reference's propagation loop body (CCSD_Helper.py:1206-1240):
-16 right-hand sides (block-frozen RK4 over T1, T2, L1, L2), the rounded state
-update and the dipole trace.  Workload: synthetic TD-CCSD at o=10, v=38
-(Q=144 seeded density-fitting integrals), dt=0.005, E(t)=0.002 sin(0.923 t).
+One RK4 "step" of one trajectory is the reference's propagation loop body
+(CCSD_Helper.py:1206-1240): 16 right-hand sides (block-frozen RK4 over T1,
+T2, L1, L2), the rounded state update and the dipole trace.
+
+Headline workload (``value``): the mixed-precision batched form at o=10,
+v=38 (Q=144 seeded density-fitting integrals), 24 trajectories advanced
+together -- 3 polarisations x A in {0.001, 0.002, 0.005, 0.01} x w0 in
+{0.5, 0.923}, E(t) = A sin(w0 t), dt = 0.005 -- from the converged ground
+state (device DIIS, 8 vectors, max residual 1e-10).  ``value`` counts
+trajectory-steps per second.  The same line reports the plain FP64 GPU form
+(one trajectory, the reference's arithmetic), the mixed form on one
+trajectory, |d mu| of the z / A=0.002 / w0=0.923 trajectory against the FP64
+form, the end-to-end rate with host buffers, the roofline of the dominant
+kernel and the CPU oracle on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision fp64|mixed|auto] [--workload NAME] [--method CCSD|CC2]
+                    [--precision fp64|mixed|auto] [--workload NAME] [--method CCSD|CC2] [--nb 24]
 
 Prints one JSON line (rank 0).  The reference arm (--impl reference) times the
 CPU oracle (the numpy restatement of the reference, all host cores) on the
-same workload; the reference itself cannot be shipped to the GPU host.
+same workload, one trajectory at a time as the reference runs them.
 """
 from __future__ import annotations
 
@@ -29,25 +39,35 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "CCSD RK4 steps/s (T+L RHS) mixed vs FP64 GPU at |Δμ|≤1e-8 au; grad/fwd cost"
-DT, A, W0 = 0.005, 0.002, 0.923
+DT = 0.005
+AMPS = (0.001, 0.002, 0.005, 0.01)
+W0S = (0.5, 0.923)
+POLS = (0, 1, 2)
+REF_TRAJ = (2, 0.002, 0.923)  # the single-trajectory configuration (z, A, w0)
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=100)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=40)
+    p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     p.add_argument("--workload", default="ccsd_o10_v38")
     p.add_argument("--method", default="CCSD", choices=["CCSD", "CC2"])
-    p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--nb", type=int, default=24, help="trajectories advanced together (24 = 3 pol x 4 A x 2 w0)")
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
 
-def start_state(sysm):
-    """MP2-guess start: t1 = 0, t2 = <ij||ab>/D, lambda = t (complex128)."""
+def trajectories(nb):
+    full = [(p, a, w) for p in POLS for a in AMPS for w in W0S]
+    return [full[k % len(full)] for k in range(nb)]
+
+
+def mp2_state(sysm):
+    """MP2-guess state: t1 = 0, t2 = <ij||ab>/D, lambda = t (complex128)."""
     from python_code_to_check_c_gb300.system import mp2_guess
     t2 = mp2_guess(sysm.tei(), sysm.eps(), sysm.o).astype(np.complex128)
     t1 = np.zeros((sysm.o, sysm.v), dtype=np.complex128)
@@ -106,10 +126,11 @@ class ClockSampler:
 
 
 def cpu_oracle_rate(sysm, method, state, budget_s=12.0, max_steps=50):
-    """Oracle (numpy restatement of the reference) RK4 steps/s on the host cores."""
+    """Oracle (numpy restatement of the reference) RK4 steps/s on the host cores,
+    the z / A=0.002 / w0=0.923 trajectory."""
     from oracle.cc_oracle import CCOracle, sin_field
     orc = CCOracle(sysm.tei(), sysm.o, mu=sysm.mu)
-    Vt = sin_field(A, W0, sysm.mu[2])
+    Vt = sin_field(REF_TRAJ[1], REF_TRAJ[2], sysm.mu[REF_TRAJ[0]])
     t = 0.0
     s = state
     t0 = time.perf_counter()
@@ -129,25 +150,49 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     from python_code_to_check_c_gb300.system import WORKLOADS, synthetic_system
-    wl = WORKLOADS[args.workload]
-    sysm = synthetic_system(**wl)
-    st = start_state(sysm)
+    sysm = synthetic_system(**WORKLOADS[args.workload], all_dipoles=True)
+    st = mp2_state(sysm)
     cores = os.cpu_count()
-    # warm-up: one step; timed: a bounded sample of the workload's steps
-    cpu_oracle_rate(sysm, args.method, st, budget_s=0.0, max_steps=1)
+    cpu_oracle_rate(sysm, args.method, st, budget_s=0.0, max_steps=1)  # warm-up
     rate, n, el = cpu_oracle_rate(sysm, args.method, st, budget_s=90.0, max_steps=max(1, args.steps))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": world,
         "steps": n, "warmup": 1, "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded DF integrals, MP2-guess start)",
-        "config": {"workload": args.workload, "method": args.method, "o": sysm.o, "v": sysm.v, "nq": sysm.nq,
-                   "dt": DT, "field": f"{A} sin({W0} t)", "parallelism": "replicas"},
+        "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded DF integrals; MP2-guess state: the cost of a step does not depend on it)",
+        "config": {"workload": f"{args.workload}_x{args.nb}", "method": args.method, "o": sysm.o, "v": sysm.v,
+                   "nq": sysm.nq, "dt": DT, "trajectories": args.nb,
+                   "note": "the reference advances one trajectory per run; trajectory-steps/s = steps/s"},
         "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{n} RK4 steps (+dipole) of {args.workload} in {el:.1f} s, numpy complex128, "
-                                   f"BLAS threads = all {cores} host cores"},
+                         "sample": f"{n} RK4 steps (+dipole) of one {args.workload} trajectory in {el:.1f} s, "
+                                   f"numpy complex128 oracle, BLAS threads = all {cores} host cores"},
         "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def ground_state(sysm, method, dev):
+    """Converged T and Lambda (device DIIS, 8 vectors, max residual 1e-10)."""
+    from python_code_to_check_c_gb300.engine import CCEngine
+    from python_code_to_check_c_gb300.system import mp2_guess
+    eng = CCEngine.from_system(sysm)
+    t2 = mp2_guess(sysm.tei(), np.linalg.eigh(sysm.fock)[0], sysm.o)
+    t1 = np.zeros((sysm.o, sysm.v))
+    E, nt, t1, t2 = eng.ground_state(method, 0, t1, t2, maxsize=8, maxiter=100, E_min=0.0, r_tol=1e-10)
+    El, nl, l1, l2 = eng.ground_state(method, 1, t1, t2, t1, t2, maxsize=8, maxiter=100, E_min=0.0, r_tol=1e-10)
+    eng.close()
+    return (t1, t2, l1, l2), {"E_corr": E, "pseudo_E": El, "t_iterations": nt, "l_iterations": nl}
+
+
+def timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    out = fn()
+    b.record()
+    torch.cuda.synchronize()
+    return out, a.elapsed_time(b)
 
 
 def run_ours(args, rank, world, local_rank):
@@ -159,10 +204,16 @@ def run_ours(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    wl = WORKLOADS[args.workload]
-    sysm = synthetic_system(**wl)
-    st = start_state(sysm)
-    eng = CCEngine.from_system(sysm)
+    sysm = synthetic_system(**WORKLOADS[args.workload], all_dipoles=True)
+    gs, gs_info = ground_state(sysm, args.method, dev)
+    nb = args.nb
+    trajs = trajectories(nb)
+    fields = [_lib.make_field("sin", a, w) for (_, a, w) in trajs]
+    pols = [p for (p, _, _) in trajs]
+    ref_k = trajs.index(REF_TRAJ) if REF_TRAJ in trajs else 0
+    bstate = [x.unsqueeze(0).expand((nb,) + tuple(x.shape)).contiguous() for x in gs]
+
+    eng = CCEngine.from_system(sysm, nb=nb)
     prec = args.precision
     if prec == "auto":
         prec = "fp64"
@@ -173,25 +224,24 @@ def run_ours(args, rank, world, local_rank):
             eng.set_precision("fp64")
     else:
         eng.set_precision(prec, 5)
-    field = _lib.make_field("sin", A, W0)
-    dst = [torch.as_tensor(x, device=dev) for x in st]
+    eng.set_fields(fields, pols)
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
     # warm-up (captures the step graphs)
-    eng.propagate(args.method, dst, 0.0, DT, max(args.warmup, 3), field)
+    eng.propagate(args.method, bstate, 0.0, DT, max(args.warmup, 3), None)
     torch.cuda.synchronize()
 
-    # ---- timed region: K device-resident steps ----
+    # ---- timed region: K device-resident steps of all nb trajectories ----
     barrier()
     torch.cuda.synchronize()
     n0 = launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clk:
         e0.record()
-        final, traj = eng.propagate(args.method, dst, 0.0, DT, args.steps, field)
+        final, traj = eng.propagate(args.method, bstate, 0.0, DT, args.steps, None)
         e1.record()
         torch.cuda.synchronize()
     barrier()
@@ -202,35 +252,41 @@ def run_ours(args, rank, world, local_rank):
         tt = torch.tensor([ms], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_max = float(tt.item())
-    value = world * args.steps / (t_max / 1e3)
+    value = world * nb * args.steps / (t_max / 1e3)
     finite = bool(torch.isfinite(torch.view_as_real(traj)).all().item())
     eng.check_errors()
 
-    # ---- the plain FP64 form on the same start state (ratio and |d mu|) ----
-    fp64 = None
+    # ---- one trajectory: the plain FP64 form and the mixed form ----
+    ref_field = _lib.make_field("sin", REF_TRAJ[1], REF_TRAJ[2])
+    e1t = CCEngine.from_system(sysm)
+    e1t.set_fields([ref_field], [REF_TRAJ[0]])
+    k1 = max(1, min(args.steps, 30))
+    e1t.set_precision("fp64")
+    e1t.propagate(args.method, gs, 0.0, DT, 3, None)
+    (_, traj64), ms64 = timed(lambda: e1t.propagate(args.method, gs, 0.0, DT, k1, None))
+    v64 = k1 / (ms64 / 1e3)
+    single_mixed = None
     if prec == "mixed":
-        k64 = max(1, min(args.steps, 30))
-        eng.set_precision("fp64")
-        eng.propagate(args.method, dst, 0.0, DT, 3, field)
-        torch.cuda.synchronize()
-        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        g0.record()
-        _, traj64 = eng.propagate(args.method, dst, 0.0, DT, k64, field)
-        g1.record()
-        torch.cuda.synchronize()
-        v64 = k64 / (g0.elapsed_time(g1) / 1e3)
-        dmu = float((traj[:k64] - traj64).abs().max().item())
-        fp64 = {"value": world * v64, "steps": k64, "mixed_over_fp64": value / (world * v64),
-                "max_dmu_vs_fp64_au": dmu, "slices": 5}
-        eng.set_precision("mixed", 5)
-        eng.propagate(args.method, dst, 0.0, DT, 1, field)
+        e1t.set_precision("mixed", 5)
+        e1t.propagate(args.method, gs, 0.0, DT, 3, None)
+        k1m = max(1, min(args.steps * 2, 100))
+        (_, _), ms1m = timed(lambda: e1t.propagate(args.method, gs, 0.0, DT, k1m, None))
+        single_mixed = {"value": k1m / (ms1m / 1e3), "unit": "steps/s", "steps": k1m}
+        e1t.check_errors()
+    e1t.close()
+    dmu = float((traj[:k1, ref_k] - traj64[:k1]).abs().max().item())
+    fp64 = {"value": world * v64, "unit": "steps/s", "steps": k1, "trajectories": 1,
+            "batched_mixed_over_fp64": value / (world * v64),
+            "max_dmu_vs_fp64_au": dmu, "dmu_steps": k1, "dmu_trajectory": "z, A=0.002, w0=0.923",
+            "slices": 5 if prec == "mixed" else None}
 
-    # ---- end-to-end through the C ABI with host buffers ----
+    # ---- end-to-end through the public API with host buffers ----
     ke = max(1, min(args.e2e_steps, args.steps))
-    hst = [torch.as_tensor(x).pin_memory() for x in st]
-    hmu = torch.empty(1, dtype=torch.complex128).pin_memory()
+    hst = [x.cpu().pin_memory() for x in bstate]
+    hmu = torch.empty(nb, dtype=torch.complex128).pin_memory()
     h2d = sum(x.numel() * x.element_size() for x in hst)
     d2h = h2d + hmu.numel() * hmu.element_size()
+    eng.propagate(args.method, [x.to(dev) for x in hst], 0.0, DT, 1, None)
     barrier()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -238,10 +294,10 @@ def run_ours(args, rank, world, local_rank):
     t_e2e = 0.0
     for i in range(ke):
         d = [x.to(dev, non_blocking=True) for x in hst]
-        new, tr = eng.propagate(args.method, d, t_e2e, DT, 1, field)
+        new, tr = eng.propagate(args.method, d, t_e2e, DT, 1, None)
         for h, x in zip(hst, new):
             h.copy_(x, non_blocking=True)
-        hmu.copy_(tr[-1:], non_blocking=True)
+        hmu.copy_(tr[-1], non_blocking=True)
         t_e2e += DT
     f1.record()
     torch.cuda.synchronize()
@@ -250,14 +306,15 @@ def run_ours(args, rank, world, local_rank):
         tt = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_ms = float(tt.item())
-    e2e = {"value": world * ke / (e2e_ms / 1e3), "unit": "steps/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "steps": ke}
+    e2e = {"value": world * nb * ke / (e2e_ms / 1e3), "unit": "steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "steps": ke, "trajectories": nb}
 
     if rank != 0:
+        eng.close()
         return
 
     # ---- roofline of the dominant kernel (CUDA events per launch) ----
-    recs = profile_step(eng, args.method, dst, 0.0, DT, field)
+    recs = profile_step(eng, args.method, bstate, 0.0, DT, fields[0])
     by = {}
     for r in recs:
         k = (r["tag"], r["backend"])
@@ -273,10 +330,14 @@ def run_ours(args, rank, world, local_rank):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
+    pairs = 15  # slice products per FP64 product with 5 slices (levels 2..6)
     if dom["kind"] == 0 and backend == 1:
         achieved = dom["flops"] / (dom["ms"] / 1e3) / 1e12
         peak = peaks.get("bf16_tflops", 1900.0)
-        roof = {"bound": "tensor", "unit": "TFLOP/s", "peak_source": "measured bf16 (MEASURED_PEAKS.json)"}
+        roof = {"bound": "tensor", "unit": "TFLOP/s",
+                "peak_source": "measured bf16 burst (MEASURED_PEAKS.json)" if "bf16_tflops" in peaks else "fallback",
+                "achieved_is": "FP64-equivalent algorithmic flops of the contraction / launch time",
+                "tensor_work_frac": achieved * pairs / peak}
     elif dom["kind"] == 0:
         achieved = dom["flops"] / (dom["ms"] / 1e3) / 1e12
         peak = 1.25
@@ -293,23 +354,27 @@ def run_ours(args, rank, world, local_rank):
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        rate, n, el = cpu_oracle_rate(sysm, args.method, st, budget_s=12.0, max_steps=20)
+        rate, n, el = cpu_oracle_rate(sysm, args.method, [x.cpu().numpy() for x in gs], budget_s=12.0, max_steps=20)
         cpu = {"value": rate, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{n} RK4 steps (+dipole) of {args.workload} in {el:.1f} s, numpy complex128 oracle, "
-                         f"BLAS threads = all host cores"}
+               "sample": f"{n} RK4 steps (+dipole) of one {args.workload} trajectory in {el:.1f} s, numpy "
+                         f"complex128 oracle, BLAS threads = all host cores"}
     ws = eng.workspace_bytes()
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == "fp64" else "bf16x5-split+f64",
-        "data": "synthetic (seeded DF integrals, MP2-guess start state)",
-        "config": {"workload": args.workload, "method": args.method, "o": sysm.o, "v": sysm.v, "nq": sysm.nq,
-                   "dt": DT, "field": f"{A} sin({W0} t)", "precision": prec, "parallelism": f"replicas x{world}",
-                   "l2": f"per-step working set {ws / 2**20:.0f} MiB workspace + "
-                         f"{sysm.n ** 4 * 8 / 2**20:.0f} MiB integrals (> 129 MB L2), no flush"},
+        "data": "synthetic (seeded DF integrals, ground state by device DIIS)",
+        "config": {"workload": f"{args.workload}_x{nb}", "method": args.method, "o": sysm.o, "v": sysm.v,
+                   "nq": sysm.nq, "dt": DT, "trajectories": nb,
+                   "fields": "A sin(w0 t), 3 pol x A {0.001,0.002,0.005,0.01} x w0 {0.5,0.923}",
+                   "value_counts": "trajectory-steps (nb per batched step)", "precision": prec,
+                   "parallelism": f"replicas x{world}",
+                   "l2": f"per-step working set {ws / 2**30:.1f} GiB workspace + "
+                         f"{sysm.n ** 4 * 8 / 2**20:.0f} MiB integrals (> 129 MB L2), no flush",
+                   "ground_state": gs_info},
         "roofline": roof, "kernel_breakdown": breakdown, "cpu_baseline": cpu, "e2e": e2e,
-        "fp64_form": fp64,
+        "fp64_form": fp64, "single_trajectory_mixed": single_mixed,
         "gpu_launches": launches, "launches_per_step": launches / args.steps, "clocks": clk.summary(),
         "finite": finite,
     }

@@ -229,13 +229,19 @@ class CCEngine:
         or (nsteps, nb) for a batched engine).  field None: the fields of
         ``set_fields``."""
         st = [to_dev(x).clone() for x in state]
-        traj = torch.empty(max(int(nsteps), 1) * self.nb, dtype=torch.complex128, device=st[0].device)
+        # a stable trajectory buffer: the captured step graphs record its address
+        need = max(int(nsteps), 1) * self.nb
+        buf = getattr(self, "_traj_buf", None)
+        if buf is None or buf.numel() < need or buf.device != st[0].device:
+            buf = torch.empty(max(need, 1024 * self.nb), dtype=torch.complex128, device=st[0].device)
+            self._traj_buf = buf
+        traj = buf
         check(self.lib.tdcc_propagate(self.handle, _lib.METHODS[method], *(_ptr(x) for x in st),
                                       float(t0), float(dt), int(nsteps), int(precs),
                                       ctypes.byref(field) if field is not None else None, _ptr(traj),
                                       _stream()),
               "tdcc_propagate")
-        traj = traj[: int(nsteps) * self.nb]
+        traj = traj[: int(nsteps) * self.nb].clone()
         return tuple(st), (traj if self.nb == 1 else traj.view(int(nsteps), self.nb))
 
 

@@ -11,7 +11,8 @@ available here, so systems are drawn from a seeded density-fitting model:
 * canonical Fock: occupied diagonal ~ U[-1.5,-0.3], virtual diagonal
   ~ U[0.2,3.0], each sorted ascending (the reference's ``eigh`` denominators
   are sorted, ``CCSD_Helper.py:327``), off-diagonal zero;
-* ``mu_z`` random symmetric with Frobenius norm 1 (x and y are zero).
+* ``mu_z`` random symmetric with Frobenius norm 1 (x and y are zero unless
+  ``all_dipoles``: then drawn the same way after mu_z).
 
 The draw order is fixed (B, occupied energies, virtual energies, mu_z) so a
 seed names a system on every platform (numpy's PCG64 streams are
@@ -50,19 +51,29 @@ class System:
         return np.diag(self.fock).copy()
 
 
-def synthetic_system(o: int, v: int, nq: int, seed: int) -> System:
+def synthetic_system(o: int, v: int, nq: int, seed: int, all_dipoles: bool = False) -> System:
+    """``all_dipoles``: also draw mu_x and mu_y (same distribution, drawn after
+    mu_z, so mu_z and everything before it are unchanged) for runs over
+    several polarisations."""
     rng = np.random.default_rng(seed)
     n = o + v
     B = rng.standard_normal((nq, n, n)) * 0.05
     B = 0.5 * (B + B.transpose(0, 2, 1))
     eo = np.sort(rng.uniform(-1.5, -0.3, o))
     ev = np.sort(rng.uniform(0.2, 3.0, v))
-    M = rng.standard_normal((n, n))
-    M = 0.5 * (M + M.T)
-    mu_z = M / np.linalg.norm(M)
+
+    def dipole():
+        M = rng.standard_normal((n, n))
+        M = 0.5 * (M + M.T)
+        return M / np.linalg.norm(M)
+
+    mu_z = dipole()
     fock = np.diag(np.concatenate([eo, ev]))
-    zero = np.zeros((n, n))
-    return System(o=o, v=v, nq=nq, seed=seed, B=B, fock=fock, mu=[zero, zero.copy(), mu_z])
+    if all_dipoles:
+        mu_x, mu_y = dipole(), dipole()
+    else:
+        mu_x, mu_y = np.zeros((n, n)), np.zeros((n, n))
+    return System(o=o, v=v, nq=nq, seed=seed, B=B, fock=fock, mu=[mu_x, mu_y, mu_z])
 
 
 def tei_from_df(B: np.ndarray) -> np.ndarray:
