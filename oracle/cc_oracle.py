@@ -34,7 +34,16 @@ import time
 import numpy as np
 
 
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
 def _ein(spec, *ops):
+    # torch tensors (the autograd cross-check of the engine's reverse-mode
+    # programs) go through torch.einsum; everything else is numpy
+    if any(_is_torch(x) for x in ops):
+        import torch
+        return torch.einsum(spec, *ops)
     return np.einsum(spec, *ops, optimize=True)
 
 
@@ -68,7 +77,7 @@ class CCOracle:
     """
 
     def __init__(self, g, o, mu=None):
-        self.g = np.asarray(g)
+        self.g = g if _is_torch(g) else np.asarray(g)
         self.n = self.g.shape[0]
         self.o = int(o)
         self.v = self.n - self.o
@@ -358,7 +367,7 @@ class CCOracle:
         r = r - _ein("ijmb,ma->ijab", wmina, l1) + _ein("ijmb,ma->ijba", wmina, l1)
         r = r + _ein("ejab,ie->ijab", weifa, l1) - _ein("ejab,ie->jiab", weifa, l1)
         x = _ein("ia,jb->ijab", l1, fme)
-        return r + x - x.transpose(0, 1, 3, 2) - x.transpose(1, 0, 2, 3) + x.transpose(1, 0, 3, 2)
+        return r + _pijab(x)
 
     # -- density and dipole (CCSD_Helper.py:984-1006, 1066-1092) ---------
     def Dij(self, t1, t2, l1, l2):

@@ -77,6 +77,7 @@ SIGNATURES = {
                             ctypes.POINTER(TdccField), _vp, _vp]),
     "tdcc_dipole_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "tdcc_program_json": (_ll, [_i, _i, _i, _i, _i, _i, ctypes.c_char_p, ctypes.c_size_t]),
+    "tdcc_adjoint_program_json": (_ll, [_i, _i, _i, _i, _i, _i, ctypes.c_char_p, ctypes.c_size_t]),
     "tdcc_profile_step": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _d, _i, ctypes.POINTER(TdccField),
                                ctypes.POINTER(TdccOpRecord), _i, ctypes.POINTER(_i)]),
 }
@@ -131,6 +132,22 @@ def program_json(o: int, v: int, method: str, block: int, n_mu: int = 3, nb: int
             return json.loads(buf.value.decode())
         if n != -6:
             raise TdccError(f"tdcc_program_json failed: {last_error()}")
+        cap *= 4
+
+
+def adjoint_program_json(o: int, v: int, method: str, block: int, n_mu: int = 3, nb: int = 1) -> dict:
+    """The reverse-mode op list of (method, block): forward slots [0, nfwd),
+    adjoint slots after them (adj_of[s] for forward slot s).  No GPU needed."""
+    import json
+    lib = load()
+    cap = 1 << 21
+    while True:
+        buf = ctypes.create_string_buffer(cap)
+        n = lib.tdcc_adjoint_program_json(o, v, METHODS[method], block, n_mu, nb, buf, cap)
+        if n >= 0:
+            return json.loads(buf.value.decode())
+        if n != -6:
+            raise TdccError(f"tdcc_adjoint_program_json failed: {last_error()}")
         cap *= 4
 
 

@@ -1050,6 +1050,17 @@ std::string program_json(const Program& p) {
              ",\"sB\":" + jarr(T.sB, a.nd) + ",\"cr\":" + jnum(T.cr) + ",\"ci\":" + jnum(T.ci) + "}";
       }
       j += "]}";
+    } else if (op.kind == OP_REDUCE) {
+      const ReduceArgs& r = op.rd;
+      j += "{\"kind\":\"reduce\",\"tag\":\"" + op.tag + "\",\"varying\":" + var +
+           ",\"out\":" + std::to_string(op.rd_out) + ",\"oout\":" + std::to_string(op.rd_oout) +
+           ",\"x\":" + std::to_string(op.rd_x) + ",\"ox\":" + std::to_string(op.rd_ox) +
+           ",\"y\":" + std::to_string(op.rd_y) + ",\"oy\":" + std::to_string(op.rd_oy) +
+           ",\"ycplx\":" + std::to_string(r.ycplx) + ",\"dout\":" + jarr(r.dout, r.no) +
+           ",\"dred\":" + jarr(r.dred, r.nr) + ",\"so_out\":" + jarr(r.so_out, r.no) +
+           ",\"so_x\":" + jarr(r.so_x, r.no) + ",\"so_y\":" + jarr(r.so_y, r.no) +
+           ",\"sr_x\":" + jarr(r.sr_x, r.nr) + ",\"sr_y\":" + jarr(r.sr_y, r.nr) +
+           ",\"cr\":" + jnum(r.cr) + ",\"ci\":" + jnum(r.ci) + ",\"acc\":" + std::to_string(r.acc) + "}";
     } else {
       j += "{\"kind\":\"trace\",\"varying\":" + var + ",\"slots\":" + jarr(op.tr_slots, 4) +
            ",\"n_mu\":" + std::to_string(op.tr_n_mu) + ",\"nb\":" + std::to_string(op.tr_nb) +
@@ -1060,6 +1071,27 @@ std::string program_json(const Program& p) {
 }
 
 }  // namespace
+
+extern "C" long long tdcc_adjoint_program_json(int o, int v, int method, int block, int n_mu, int nb, char* buf,
+                                               size_t len) {
+  if (o < 1 || v < 1 || !valid_method(method) || block < 0 || block > 4 || n_mu < 1 || n_mu > 3 || nb < 1)
+    return fail(TDCC_ERR_ARG, "bad arguments");
+  try {
+    Program p(Dims{o, v, o + v}, "introspect");
+    build_program(p, method, block, n_mu, nb);
+    Program a(p.dims, "introspect_adj");
+    std::vector<int> adj_of;
+    build_adjoint(p, a, adj_of);
+    std::string j = program_json(a);
+    j.pop_back();  // '}'
+    j += ",\"nfwd\":" + std::to_string(p.slots.size()) + ",\"adj_of\":" + jarr(adj_of.data(), (int)adj_of.size()) + "}";
+    if (!buf || len < j.size() + 1) return fail(TDCC_ERR_LIMIT, "buffer too small: need " + std::to_string(j.size() + 1));
+    memcpy(buf, j.c_str(), j.size() + 1);
+    return (long long)j.size();
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_ARG, ex.what());
+  }
+}
 
 extern "C" long long tdcc_program_json(int o, int v, int method, int block, int n_mu, int nb, char* buf,
                                        size_t len) {

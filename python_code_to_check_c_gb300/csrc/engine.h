@@ -112,7 +112,25 @@ struct Term {
   View B;  // slot -1: absent
 };
 
-enum OpKind { OP_GEMM = 0, OP_ADD = 1, OP_TRACE = 2, OP_PACK = 3, OP_TCGEMM = 4 };
+enum OpKind { OP_GEMM = 0, OP_ADD = 1, OP_TRACE = 2, OP_PACK = 3, OP_TCGEMM = 4, OP_REDUCE = 5 };
+
+// out[o] (+)= c * sum_r X[o, r] (* Y[o, r]) over strided index spaces: the
+// adjoint of an elementwise term whose operand is broadcast (outer products,
+// scaled rows).  Complex X and out; Y complex or real, or absent.
+constexpr int kRedDims = 6;
+struct ReduceArgs {
+  void* out;
+  const void* X;
+  const void* Y;
+  int no, nr;                 // output / reduction dimensions
+  int dout[kRedDims], dred[kRedDims];
+  long long so_out[kRedDims], so_x[kRedDims], so_y[kRedDims];  // strides of the output dims
+  long long sr_x[kRedDims], sr_y[kRedDims];                    // strides of the reduction dims
+  long long nout, nred;
+  int ycplx;
+  double cr, ci;
+  int acc;
+};
 
 // Tensor-core backend argument blocks (gemm_tc.cu).
 struct PackArgs {
@@ -183,6 +201,10 @@ struct Op {
   PackArgs pk{};
   int pk_src = -1, pk_dt = R64, pk_dst = -1;
   long long pk_off = 0, pk_exp_off = 0;
+  // REDUCE: out / X / Y slots and offsets
+  ReduceArgs rd{};
+  int rd_out = -1, rd_x = -1, rd_y = -1;
+  long long rd_oout = 0, rd_ox = 0, rd_oy = 0;
   // TCGEMM: packed A / B slots, output C, error-flag slot
   TcArgs tc{};
   int tc_pa = -1, tc_pb = -1, tc_err = -1;
@@ -308,6 +330,16 @@ class Program {
 // merges contiguous dimensions of an elementwise op (program.cpp)
 void coalesce(AddArgs& a);
 
+// Reverse-mode (vector-Jacobian product) program of `f` (adjoint.cpp).
+// `f` must be batched and analysed but not yet backend-selected.  The
+// adjoint program shares f's slots [0, f.slots.size()) (bound to the same
+// memory) and adds one adjoint slot per differentiable slot; adj_of[s] is
+// the adjoint slot of forward slot s (-1: not differentiable).  Adjoints are
+// carried conjugated (a = conj(dJ/dRe z + i dJ/dIm z)), so every op of the
+// holomorphic equations maps to plain transposed products.  Each generated
+// op inherits the varying / constant flags of the forward op it reverses.
+void build_adjoint(const Program& f, Program& a, std::vector<int>& adj_of);
+
 // FP64 contraction tile shapes (kernels.cu)
 constexpr int kNumTiles = 5;
 extern const int kTiles[kNumTiles][2];
@@ -319,6 +351,7 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st);
 cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st);
 bool tc_available();
 cudaError_t launch_add(const AddArgs& a, cudaStream_t st);
+cudaError_t launch_reduce(const ReduceArgs& r, cudaStream_t st);
 cudaError_t launch_trace(int n, int o, int n_mu, const double* mu, const void* dij,
                          const void* l1, const void* dai, const void* dab, void* res, int nb,
                          const long long* bs, long long bsres, cudaStream_t st);

@@ -339,6 +339,70 @@ cudaError_t launch_add(const AddArgs& a, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// reduction: out[o] (+)= c * sum_r X[o, r] (* Y[o, r]).  One warp per output
+// element, lanes over the reduction index, fixed-order shuffle sum.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long red_off(const int* d, const long long* s, int nd, long long l) {
+  long long off = 0;
+#pragma unroll
+  for (int q = kRedDims - 1; q >= 0; --q) {
+    if (q < nd) {
+      off += (l % d[q]) * s[q];
+      l /= d[q];
+    }
+  }
+  return off;
+}
+
+__global__ void __launch_bounds__(256) reduce_kernel(const ReduceArgs r) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < r.nout; w += nw) {
+    const long long oo = red_off(r.dout, r.so_out, r.no, w);
+    const long long ox = red_off(r.dout, r.so_x, r.no, w);
+    const long long oy = red_off(r.dout, r.so_y, r.no, w);
+    double sr = 0.0, si = 0.0;
+    for (long long k = lane; k < r.nred; k += 32) {
+      const double2 x = static_cast<const double2*>(r.X)[ox + red_off(r.dred, r.sr_x, r.nr, k)];
+      double2 v = x;
+      if (r.Y) {
+        const long long yo = oy + red_off(r.dred, r.sr_y, r.nr, k);
+        const double2 y = ld(r.Y, yo, r.ycplx);
+        v = make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+      }
+      sr += v.x;
+      si += v.y;
+    }
+    for (int dd = 16; dd > 0; dd >>= 1) {
+      sr += __shfl_down_sync(0xffffffffu, sr, dd);
+      si += __shfl_down_sync(0xffffffffu, si, dd);
+    }
+    if (lane == 0) {
+      double2* out = static_cast<double2*>(r.out);
+      const double vr = r.cr * sr - r.ci * si, vi = r.cr * si + r.ci * sr;
+      if (r.acc) {
+        double2 c = out[oo];
+        c.x += vr;
+        c.y += vi;
+        out[oo] = c;
+      } else {
+        out[oo] = make_double2(vr, vi);
+      }
+    }
+  }
+}
+
+cudaError_t launch_reduce(const ReduceArgs& r, cudaStream_t st) {
+  if (r.nout <= 0) return cudaSuccess;
+  if (r.no < 0 || r.no > kRedDims || r.nr < 0 || r.nr > kRedDims) return cudaErrorInvalidValue;
+  long long blocks = (r.nout + 7) / 8;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(r);
+  count_launch();
+  return cudaGetLastError();
+}
+
 struct TraceBatch {
   long long bs[4];  // batch strides of Dij, l1, Dai, Dab (elements)
   long long bsres;

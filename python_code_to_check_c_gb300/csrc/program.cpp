@@ -643,6 +643,12 @@ cudaError_t Program::launch_op(const Op& op, const std::vector<void*>& bases, cu
     p.out = dst;
     p.exps = reinterpret_cast<int*>(dst + op.pk_exp_off);
     e = launch_pack(p, st);
+  } else if (op.kind == OP_REDUCE) {
+    ReduceArgs r = op.rd;
+    r.out = const_cast<void*>(at(bases, op.rd_out, op.rd_oout, C64));
+    r.X = at(bases, op.rd_x, op.rd_ox, C64);
+    r.Y = op.rd_y >= 0 ? at(bases, op.rd_y, op.rd_oy, r.ycplx ? C64 : R64) : nullptr;
+    e = launch_reduce(r, st);
   } else if (op.kind == OP_TCGEMM) {
     TcArgs a = op.tc;
     const char* pa = static_cast<const char*>(bases[op.tc_pa]);
@@ -836,6 +842,8 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
       return ws_dims(nm, 1, d1, U8).slot;
     };
     Op pa, pb, t;
+    pa.varying = pb.varying = t.varying = op.varying;  // phases of reverse-mode programs
+    pa.is_const = pb.is_const = t.is_const = op.is_const;
     pa.kind = pb.kind = OP_PACK;
     pa.tag = op.tag + ":packA";
     pb.tag = op.tag + ":packB";
@@ -883,7 +891,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
                               std::to_string(pk.pk_dt) + "|" + group_key(gr, false) + "|" +
                               group_key(gk, k_s1) + "|" + std::to_string(rows) + "x" + std::to_string(Kp) +
                               "s" + std::to_string(S) + "b" + std::to_string(pk.pk.nb) + ":" +
-                              std::to_string(pk.pk.bs);
+                              std::to_string(pk.pk.bs) + (op.varying ? "v" : "p") + (op.is_const ? "c" : "");
       auto it = pack_cache.find(key);
       if (it != pack_cache.end() && last_write[it->second.src] < (long long)it->second.pos) {
         pk.pk_dst = it->second.slot;
@@ -982,6 +990,8 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     if (a.atomic && !a.acc) {
       // zero the output first: its modes are the M and N groups (strides s1)
       Op z;
+      z.varying = op.varying;
+      z.is_const = op.is_const;
       z.kind = OP_ADD;
       z.tag = op.tag + ":zero";
       AddArgs& za = z.a;

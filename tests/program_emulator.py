@@ -83,6 +83,27 @@ class Emulator:
         else:
             C[offc] = s
 
+    def _reduce(self, op):
+        out = self.bufs[op["out"]]
+        X = self.bufs[op["x"]]
+        Y = self.bufs[op["y"]] if op["y"] >= 0 else None
+        do, dr = op["dout"], op["dred"]
+        Io = np.indices(do).reshape(len(do), -1).astype(np.int64) if do else np.zeros((0, 1), np.int64)
+        Ir = np.indices(dr).reshape(len(dr), -1).astype(np.int64) if dr else np.zeros((0, 1), np.int64)
+        def off(I, s):
+            return (I * np.array(s, dtype=np.int64)[:, None]).sum(0) if len(s) else np.zeros(I.shape[1], np.int64)
+        xo = op["ox"] + off(Io, op["so_x"])[:, None] + off(Ir, op["sr_x"])[None, :]
+        v = X[xo].astype(np.complex128)
+        if Y is not None:
+            yo = op["oy"] + off(Io, op["so_y"])[:, None] + off(Ir, op["sr_y"])[None, :]
+            v = v * Y[yo]
+        r = complex(op["cr"], op["ci"]) * v.sum(1)
+        oo = op["oout"] + off(Io, op["so_out"])
+        if op["acc"]:
+            out[oo] += r
+        else:
+            out[oo] = r
+
     def _trace(self, op):
         o, v, n = self.o, self.v, self.n
         dij, l1, dai, dab = (self.bufs[k] for k in op["slots"])
