@@ -200,6 +200,36 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
                    double t0, double dt, int nsteps, int precs,
                    const tdcc_field* field, void* mu_traj, void* stream);
 
+/* Gradient of a dipole-response objective with respect to the field, by
+   reverse mode through tdcc_propagate's steps (no counterpart in the
+   reference).  J_b = sum_n w[n] Re mu_b(t_n) over the recorded dipole of
+   trajectory b after step n (n = 0..nsteps-1, the trajectory tdcc_propagate
+   records).  Writes J_out[b] (host double[nb]) and gE_host (host
+   complex128 as interleaved doubles, [nsteps][4][nb]): the derivative of J_b
+   with respect to the field value at each right-hand-side evaluation of step
+   n -- RK4 stage s = 0..3 at t, t + dt/2, t + dt/2, t + dt with t the step's
+   time (t0 advanced n + 1 times by dt) -- so that for any real parameter
+   theta of the field dJ_b/dtheta = sum_{n,s} Re(gE[n][s][b] dE_b(tau)/dtheta).
+   If a_t1..a_l2 are not NULL they receive dJ/d(initial state) (conjugated:
+   conj(dJ/dRe + i dJ/dIm)).  The forward runs the captured step graphs and
+   keeps the state every `checkpoint` steps; the backward recomputes each
+   segment and runs the generated reverse-mode programs (the vector-Jacobian
+   products of the right-hand sides).  The rounding of the state (precs >= 0)
+   is taken as the identity; precs < 0 makes the map smooth.  Synchronous;
+   allocates its checkpoint and segment storage for the duration of the call.
+   Fields: `field` for every trajectory, or tdcc_set_fields when NULL.      */
+int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, const void* l1,
+                 const void* l2, double t0, double dt, int nsteps, int precs,
+                 const tdcc_field* field, const double* w_host, int checkpoint,
+                 double* J_out, double* gE_host, void* a_t1, void* a_t2, void* a_l1,
+                 void* a_l2, void* stream);
+
+/* Reverse-mode op list of (method, block) as JSON (like tdcc_program_json):
+   forward slots [0, nfwd), adjoint slots after them, "adj_of" maps each
+   forward slot to its adjoint slot (-1: not differentiable).  No GPU.     */
+long long tdcc_adjoint_program_json(int o, int v, int method, int block, int n_mu, int nb,
+                                    char* buf, size_t len);
+
 /* Dipole expectation value like tdcc_dipole, but without allocating any
    device memory and without a tdcc_system.  No counterpart in the reference
    (its dipole_moment, CCSD_Helper.py:1066, allocates numpy temporaries).

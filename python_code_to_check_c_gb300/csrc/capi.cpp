@@ -33,6 +33,7 @@ bool tc_available();
 struct ProgInst {
   std::unique_ptr<Program> prog;
   std::vector<void*> bases;
+  size_t nfwd = 0;           // reverse-mode programs: slots [0, nfwd) are the forward program's
   std::vector<void*> owned;  // this program's workspace allocations
   long long bytes = 0;
   bool setup_done = false;   // integral-only ops (e.g. packed integral blocks) ran
@@ -48,8 +49,26 @@ struct ProgInst {
     dag.destroy();
     for (void* p : owned) cudaFree(p);
   }
+  // every slot an op of the program touches must be bound (checked on the
+  // host before each run: an unbound slot would be a null device pointer)
+  std::vector<int> used;
+  void check_bound() {
+    if (used.empty()) {
+      std::vector<char> u(prog->slots.size(), 0);
+      for (const auto& op : prog->ops) {
+        for (int r : op.reads)
+          if (r >= 0) u[r] = 1;
+        if (op.write >= 0) u[op.write] = 1;
+      }
+      for (size_t i = 0; i < u.size(); ++i)
+        if (u[i]) used.push_back((int)i);
+    }
+    for (int i : used)
+      if (!bases[i]) throw std::runtime_error("unbound buffer slot " + prog->slots[i].name + " in " + prog->name);
+  }
   // phase ops as a dependency DAG (serially, in program order, when timed)
   cudaError_t exec(cudaStream_t st, Program::Phase ph, std::vector<Program::Timed>* timed = nullptr) {
+    check_bound();
     // TDCC_SERIAL=1 issues every op in program order on `st` (debugging aid)
     static const bool serial = [] {
       const char* e = getenv("TDCC_SERIAL");
@@ -85,6 +104,8 @@ struct tdcc_system_s {
   std::vector<int> h_pol;
   std::unique_ptr<ProgInst> rhs[2][4];
   std::unique_ptr<ProgInst> dens;
+  std::unique_ptr<ProgInst> adjp[2][5];  // reverse-mode programs (block 4: density)
+  std::vector<int> adj_of[2][5];         // adjoint slot of each forward slot
   std::vector<void*> owned;
   long long ws_bytes = 0;
 
@@ -196,6 +217,33 @@ ProgInst& get_density(tdcc_system s) {
   return *s->dens;
 }
 
+void build_program(Program& p, int method, int block, int n_mu, int nb);
+
+// Reverse-mode program of (method, block); block 4 = density.  Its slots
+// [0, nfwd) are bound to the forward instance's buffers before every run.
+ProgInst& get_adj(tdcc_system s, int method, int block) {
+  auto& slot = s->adjp[method][block];
+  if (slot) return *slot;
+  if (block == 4)
+    get_density(s);
+  else
+    get_rhs(s, method, block);
+  Program f(s->dims, "fwd");
+  build_program(f, method, block, s->n_mu, s->nb);
+  auto pi = std::make_unique<ProgInst>();
+  pi->prog = std::make_unique<Program>(s->dims, "adj");
+  build_adjoint(f, *pi->prog, s->adj_of[method][block]);
+  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
+  pi->nfwd = f.slots.size();
+  pi->bases.assign(pi->prog->slots.size(), nullptr);
+  pi->bytes = pi->prog->allocate(pi->bases, pi->owned, pi->nfwd, true);
+  s->ws_bytes += pi->bytes;
+  pi->setup_done = true;  // no integral-only ops in a reverse-mode program
+  pi->dag.init(pi->prog->ops.size(), 4);
+  slot = std::move(pi);
+  return *slot;
+}
+
 void ensure_rk(tdcc_system s) {
   if (s->rk_ready) return;
   const long long n = s->dims.n;
@@ -260,7 +308,7 @@ void timed_launch(Prof* pf, cudaStream_t st, const char* tag, int block, int sta
 
 // One RK4 block (ft1/ft2/fL1/fL2): prologue once, four stages, final update.
 void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* out_b, double dt,
-               int precs, cudaStream_t st, Prof* pf = nullptr) {
+               int precs, cudaStream_t st, Prof* pf = nullptr, double2* const* store = nullptr) {
   ProgInst& pi = get_rhs(s, method, b);
   Program& p = *pi.prog;
   auto& B = pi.bases;
@@ -282,6 +330,9 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
     const double h = stage < 3 ? dt / 2.0 : dt;
     timed_launch(pf, st, "rk4_stage_axpy", b, stage, (double)n * 16 * (stage == 1 ? 3 : stage == 4 ? 3 : 5),
                  [&] { return launch_rk4_stage(in[b], s->kbuf[b], s->acc[b], s->yin[b], n, stage, h, st); });
+    // the input of stage + 1 (reverse mode recomputes each stage from it)
+    if (store && stage < 4)
+      CK(cudaMemcpyAsync(store[stage - 1], s->yin[b], n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
   }
   const int sign = (b == TDCC_T1 || b == TDCC_T2) ? -1 : +1;
   const double scale = precs >= 0 ? std::pow(10.0, (double)precs) : 1.0;
@@ -294,19 +345,22 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
 // new state.  `in` and `out` must not alias.  With a profiler everything
 // runs serially on s->main.
 void run_step(tdcc_system s, int method, double2* const in[4], double2* const out[4], double dt,
-              int precs, double2* traj, Prof* pf = nullptr) {
+              int precs, double2* traj, Prof* pf = nullptr, double2* const* store = nullptr,
+              double2* fs_store = nullptr) {
   cudaStream_t m = s->main;
   const long long nn = (long long)s->dims.n * s->dims.n;
   timed_launch(pf, m, "advance_field", 5, 0, 0.0, [&] { return launch_advance_field(s->ctx, s->nb, m); });
   timed_launch(pf, m, "dress_fock", 5, 0, (double)nn * (8 + 8 * s->nb + 3 * 16 * s->nb),
                [&] { return launch_dress(s->ctx, s->fock, s->mu, s->Fs, s->dims.n, s->nb, m); });
+  if (fs_store)
+    CK(cudaMemcpyAsync(fs_store, s->Fs, 3 * (size_t)s->nb * nn * sizeof(double2), cudaMemcpyDeviceToDevice, m));
   if (pf) {
     for (int b = 0; b < 4; ++b) run_block(s, method, b, in, out[b], dt, precs, m, pf);
   } else {
     CK(cudaEventRecord(s->ev_fork, m));
     for (int b = 0; b < 4; ++b) {
       CK(cudaStreamWaitEvent(s->bs[b], s->ev_fork, 0));
-      run_block(s, method, b, in, out[b], dt, precs, s->bs[b]);
+      run_block(s, method, b, in, out[b], dt, precs, s->bs[b], nullptr, store ? store + 3 * b : nullptr);
       CK(cudaEventRecord(s->ev_join[b], s->bs[b]));
     }
     for (int b = 0; b < 4; ++b) CK(cudaStreamWaitEvent(m, s->ev_join[b], 0));
@@ -373,6 +427,12 @@ void reset_programs(tdcc_system s) {
     s->ws_bytes -= s->dens->bytes;
     s->dens.reset();
   }
+  for (auto& mrow : s->adjp)
+    for (auto& pi : mrow)
+      if (pi) {
+        s->ws_bytes -= pi->bytes;
+        pi.reset();
+      }
   for (auto& g : s->gexec)
     if (g) {
       cudaGraphExecDestroy(g);
@@ -725,8 +785,8 @@ int tdcc_check_errors(tdcc_system s) {
   const cudaError_t ce = cudaDeviceSynchronize();
   if (ce != cudaSuccess) return fail(TDCC_ERR_CUDA, std::string("device error: ") + cudaGetErrorString(ce));
   for (int m = 0; m < 2; ++m)
-    for (int b = 0; b < 4; ++b) {
-      auto& pi = s->rhs[m][b];
+    for (int b = 0; b < 9; ++b) {
+      auto& pi = b < 4 ? s->rhs[m][b] : s->adjp[m][b - 4];
       if (!pi || pi->prog->err_slot < 0) continue;
       int flag = 0;
       void* p = pi->bases[pi->prog->err_slot];
@@ -821,9 +881,14 @@ int tdcc_rk4_step(tdcc_system s, int method, const void* t1, const void* t2, con
   return TDCC_OK;
 }
 
-int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void* l2, double t0,
-                   double dt, int nsteps, int precs, const tdcc_field* field, void* mu_traj,
-                   void* stream) {
+}  // extern "C"
+
+namespace {
+// tdcc_propagate, optionally copying the state at steps 0, ck_every, 2 ck_every, ...
+// (before those steps) into ck[4 * j + block].
+int propagate_impl(tdcc_system s, int method, void* t1, void* t2, void* l1, void* l2, double t0, double dt,
+                   int nsteps, int precs, const tdcc_field* field, void* mu_traj, void* stream, int ck_every,
+                   double2* const* ck) {
   if (!s) return fail(TDCC_ERR_ARG, "null system");
   if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
   if (!t1 || !t2 || !l1 || !l2 || !mu_traj) return fail(TDCC_ERR_ARG, "NULL argument");
@@ -887,6 +952,10 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
     CK(cudaEventRecord(s->ev_user, s->main));
     CK(cudaStreamWaitEvent(user, s->ev_user, 0));
     for (int i = 0; i < nsteps; ++i) {
+      if (ck && i % ck_every == 0)
+        for (int b = 0; b < 4; ++b)
+          CK(cudaMemcpyAsync(ck[4 * (i / ck_every) + b], s->st[i & 1][b], s->nelb(b) * sizeof(double2),
+                             cudaMemcpyDeviceToDevice, user));
       CK(cudaGraphLaunch(s->gexec[i & 1], user));
       count_launch(s->g_nodes[i & 1]);
     }
@@ -903,6 +972,185 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
           return fail(TDCC_ERR_NONFINITE, "dipole of trajectory " + std::to_string(b) +
                                               " is not finite after propagation");
     }
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  return TDCC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void* l2, double t0,
+                   double dt, int nsteps, int precs, const tdcc_field* field, void* mu_traj,
+                   void* stream) {
+  return propagate_impl(s, method, t1, t2, l1, l2, t0, dt, nsteps, precs, field, mu_traj, stream, 1, nullptr);
+}
+
+int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, const void* l1, const void* l2,
+                 double t0, double dt, int nsteps, int precs, const tdcc_field* field, const double* w_host,
+                 int checkpoint, double* J_out, double* gE_host, void* a_t1, void* a_t2, void* a_l1, void* a_l2,
+                 void* stream) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
+  if (!t1 || !t2 || !l1 || !l2 || !w_host || !J_out || !gE_host) return fail(TDCC_ERR_ARG, "NULL argument");
+  if (nsteps < 1 || !(dt > 0.0)) return fail(TDCC_ERR_ARG, "nsteps >= 1 and dt > 0 required");
+  if (checkpoint < 1) return fail(TDCC_ERR_ARG, "checkpoint interval must be >= 1");
+  if (precs > 22) return fail(TDCC_ERR_ARG, "precs must be <= 22");
+  const int K = std::min(checkpoint, nsteps), nseg = (nsteps + K - 1) / K;
+  const int nb = s->nb, n_mu = s->n_mu, n = s->dims.n;
+  const long long nn = (long long)n * n;
+  std::vector<void*> mem;
+  struct Guard {
+    std::vector<void*>& m;
+    ~Guard() {
+      cudaDeviceSynchronize();
+      for (void* p : m) cudaFree(p);
+    }
+  } guard{mem};
+  auto alloc = [&](size_t bytes) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::runtime_error("cudaMalloc of " + std::to_string(bytes) + " bytes failed (adjoint)");
+    }
+    mem.push_back(p);
+    return static_cast<double2*>(p);
+  };
+  try {
+    ensure_rk(s);
+    for (int b = 0; b < 4; ++b) {
+      get_adj(s, method, b);
+      CK(get_rhs(s, method, b).setup(s->main));
+    }
+    get_adj(s, method, 4);
+    cudaStream_t user = static_cast<cudaStream_t>(stream), m = s->main;
+    CK(cudaEventRecord(s->ev_user, user));
+    CK(cudaStreamWaitEvent(m, s->ev_user, 0));
+    auto nel = [&](int b) { return (size_t)s->nelb(b); };
+    const size_t maxel = nel(1);
+    // ---- working memory for the call ----
+    std::vector<double2*> ck(4 * nseg), y(4), segY(4 * (K + 1)), segSt(12 * K), segFs(K), ay(4), ay2(4), ak(4);
+    for (int j = 0; j < nseg; ++j)
+      for (int b = 0; b < 4; ++b) ck[4 * j + b] = alloc(nel(b) * 16);
+    for (int b = 0; b < 4; ++b) y[b] = alloc(nel(b) * 16);
+    for (int k = 0; k <= K; ++k)
+      for (int b = 0; b < 4; ++b) segY[4 * k + b] = alloc(nel(b) * 16);
+    for (int k = 0; k < K; ++k) {
+      for (int b = 0; b < 4; ++b)
+        for (int q = 0; q < 3; ++q) segSt[12 * k + 3 * b + q] = alloc(nel(b) * 16);
+      segFs[k] = alloc(3 * (size_t)nb * nn * 16);
+    }
+    for (int b = 0; b < 4; ++b) {
+      ay[b] = alloc(nel(b) * 16);
+      ay2[b] = alloc(nel(b) * 16);
+      ak[b] = alloc(maxel * 16);
+    }
+    double2* akin = alloc(maxel * 16);
+    double2* aY = alloc(maxel * 16);
+    double2* aF = alloc((size_t)nb * nn * 16);
+    double2* ares = alloc((size_t)nb * n_mu * 16);
+    double2* gE = alloc((size_t)nsteps * 4 * nb * 16);
+    double2* traj = alloc((size_t)nsteps * nb * 16);
+    CK(cudaMemsetAsync(gE, 0, (size_t)nsteps * 4 * nb * 16, m));
+    const void* in[4] = {t1, t2, l1, l2};
+    for (int b = 0; b < 4; ++b) CK(cudaMemcpyAsync(y[b], in[b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
+    CK(cudaStreamSynchronize(m));
+
+    // ---- forward: the captured step graphs, checkpoints every K steps ----
+    const int rc = propagate_impl(s, method, y[0], y[1], y[2], y[3], t0, dt, nsteps, precs, field, traj, m, K,
+                                  ck.data());
+    if (rc != TDCC_OK) return rc;
+    {
+      std::vector<double2> ht((size_t)nsteps * nb);
+      CK(cudaMemcpy(ht.data(), traj, ht.size() * 16, cudaMemcpyDeviceToHost));
+      for (int b = 0; b < nb; ++b) {
+        double J = 0.0;
+        for (int i = 0; i < nsteps; ++i) J += w_host[i] * ht[(size_t)i * nb + b].x;
+        J_out[b] = J;
+      }
+    }
+
+    // ---- backward, segment by segment ----
+    for (int b = 0; b < 4; ++b) CK(cudaMemsetAsync(ay[b], 0, nel(b) * 16, m));
+    const double c6 = dt / 6.0;
+    const double wst[4] = {1.0, 2.0, 2.0, 1.0};
+    const double hst[4] = {0.0, dt / 2.0, dt / 2.0, dt};  // Y(s) = y + h_s k_(s-1)
+    for (int j = nseg - 1; j >= 0; --j) {
+      const int k0 = j * K, kn = std::min(K, nsteps - k0);
+      double tk = t0;
+      for (int i = 0; i < k0; ++i) tk += dt;  // the forward's time accumulation
+      for (int b = 0; b < 4; ++b)
+        CK(cudaMemcpyAsync(segY[b], ck[4 * j + b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
+      set_ctx(s, tk, dt, field, m);
+      for (int k = 0; k < kn; ++k)
+        run_step(s, method, &segY[4 * k], &segY[4 * (k + 1)], dt, precs, nullptr, nullptr, &segSt[12 * k],
+                 segFs[k]);
+      for (int k = kn - 1; k >= 0; --k) {
+        const int nstep = k0 + k;
+        // the objective's dipole term at y_(n+1)
+        if (w_host[nstep] != 0.0) {
+          ProgInst& d = get_density(s);
+          ProgInst& ad = get_adj(s, method, 4);
+          const auto& aof = s->adj_of[method][4];
+          for (int q = 0; q < 4; ++q) d.bases[S_T1 + q] = segY[4 * (k + 1) + q];
+          d.bases[S_RES] = s->res;
+          CK(d.exec(m, Program::ALL));
+          for (size_t i = 0; i < ad.nfwd; ++i) ad.bases[i] = d.bases[i];
+          CK(launch_dipole_cotangent(ares, s->d_pol, nb, n_mu, w_host[nstep], m));
+          ad.bases[aof[S_RES]] = ares;
+          for (int q = 0; q < 4; ++q)
+            if (aof[S_T1 + q] >= 0) ad.bases[aof[S_T1 + q]] = ay[q];
+          CK(ad.exec(m, Program::ALL));
+        }
+        // step adjoint: ay (of y_(n+1)) -> ay2 (of y_n); rounding taken as the identity
+        for (int q = 0; q < 4; ++q) CK(cudaMemcpyAsync(ay2[q], ay[q], nel(q) * 16, cudaMemcpyDeviceToDevice, m));
+        for (int b = 0; b < 4; ++b) {
+          ProgInst& pi = get_rhs(s, method, b);
+          ProgInst& ai = get_adj(s, method, b);
+          const auto& aof = s->adj_of[method][b];
+          auto& B = pi.bases;
+          for (int q = 0; q < 4; ++q) B[S_T1 + q] = segY[4 * k + q];
+          B[S_OUT] = s->kbuf[b];
+          B[S_F] = segFs[k];
+          CK(pi.exec(m, Program::PROLOGUE));
+          // a_k(s) = c w_s a_out, c = -i dt/6 (T) or +i dt/6 (Lambda)
+          const double ci = (b == TDCC_T1 || b == TDCC_T2) ? -c6 : c6;
+          for (int st = 0; st < 4; ++st) CK(launch_caxpy(ak[st], ay[b], nel(b), 0.0, wst[st] * ci, 0, m));
+          for (int st = 4; st >= 1; --st) {
+            B[S_T1 + b] = st == 1 ? segY[4 * k + b] : segSt[12 * k + 3 * b + (st - 2)];
+            B[S_F] = segFs[k] + (size_t)(st == 1 ? 0 : st < 4 ? 1 : 2) * nb * nn;
+            CK(pi.exec(m, Program::STAGE));
+            for (size_t i = 0; i < ai.nfwd; ++i) ai.bases[i] = B[i];
+            CK(cudaMemcpyAsync(akin, ak[st - 1], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
+            ai.bases[aof[S_OUT]] = akin;
+            CK(cudaMemsetAsync(aY, 0, nel(b) * 16, m));
+            if (aof[S_T1 + b] >= 0) ai.bases[aof[S_T1 + b]] = aY;
+            if (aof[S_F] >= 0) {
+              CK(cudaMemsetAsync(aF, 0, (size_t)nb * nn * 16, m));
+              ai.bases[aof[S_F]] = aF;
+            }
+            for (int q = 0; q < 4; ++q)
+              if (q != b && aof[S_T1 + q] >= 0) ai.bases[aof[S_T1 + q]] = ay2[q];
+            CK(ai.exec(m, Program::STAGE));
+            if (aof[S_F] >= 0)
+              CK(launch_field_grad(aF, s->mu, s->d_pol, n, nb, gE + ((size_t)nstep * 4 + (st - 1)) * nb, m));
+            CK(launch_caxpy(ay2[b], aY, nel(b), 1.0, 0.0, 1, m));
+            if (st > 1) CK(launch_caxpy(ak[st - 2], aY, nel(b), hst[st - 1], 0.0, 1, m));
+          }
+          CK(ai.exec(m, Program::PROLOGUE));
+        }
+        std::swap(ay, ay2);
+      }
+    }
+    void* aout[4] = {a_t1, a_t2, a_l1, a_l2};
+    for (int b = 0; b < 4; ++b)
+      if (aout[b]) CK(cudaMemcpyAsync(aout[b], ay[b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
+    CK(cudaMemcpyAsync(gE_host, gE, (size_t)nsteps * 4 * nb * 16, cudaMemcpyDeviceToHost, m));
+    CK(cudaStreamSynchronize(m));
+    CK(cudaEventRecord(s->ev_user, m));
+    CK(cudaStreamWaitEvent(user, s->ev_user, 0));
   } catch (const std::exception& ex) {
     return fail(TDCC_ERR_CUDA, ex.what());
   }

@@ -297,8 +297,9 @@ class Program {
   // tile shape and split-K of a contraction from its extents
   static void plan_gemm(Op& op, bool allow_split);
 
-  // device allocation of workspace slots (returns bytes allocated)
-  long long allocate(std::vector<void*>& bases, std::vector<void*>& owned);
+  // device allocation of the non-fixed slots from index `first` on (returns
+  // bytes allocated); `zero`: clear them (accumulators of adjoint programs)
+  long long allocate(std::vector<void*>& bases, std::vector<void*>& owned, size_t first = 0, bool zero = false);
 
   // ALL: every op.  SETUP: ops that depend on the integrals only (once per
   // system).  PROLOGUE: the rest of the ops independent of the varying

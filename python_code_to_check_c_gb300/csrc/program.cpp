@@ -577,10 +577,11 @@ void Program::batch(int nbt) {
   }
 }
 
-long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned) {
+long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned, size_t first, bool zero) {
   long long bytes = 0;
   if (bases.size() < slots.size()) bases.resize(slots.size(), nullptr);
-  for (size_t i = kNumFixedSlots; i < slots.size(); ++i) {
+  for (size_t i = std::max<size_t>(first, kNumFixedSlots); i < slots.size(); ++i) {
+    if (slots[i].fixed) continue;
     const size_t b = (size_t)slots[i].numel * (size_t)elem_bytes(slots[i].dt);
     void* p = nullptr;
     if (cudaMalloc(&p, b) != cudaSuccess) {
@@ -589,6 +590,7 @@ long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned
     }
     owned.push_back(p);
     bases[i] = p;
+    if (zero && cudaMemset(p, 0, b) != cudaSuccess) throw std::runtime_error("zeroing workspace " + slots[i].name + " failed");
     if (!slots[i].init.empty() &&
         cudaMemcpy(p, slots[i].init.data(), slots[i].init.size() * sizeof(double),
                    cudaMemcpyHostToDevice) != cudaSuccess)

@@ -132,6 +132,88 @@ __global__ void record_mu_kernel(StepCtx* ctx, const double2* res, double2* traj
   }
 }
 
+// ---------------------------------------------------------------------------
+// reverse-mode helpers (tdcc_adjoint)
+// ---------------------------------------------------------------------------
+// y = c x  (acc = 0) or y += c x  (acc = 1), complex c
+__global__ void caxpy_kernel(double2* __restrict__ y, const double2* __restrict__ x, long long n, double cr, double ci,
+                             int acc) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = x[i];
+    const double2 p = make_double2(cr * v.x - ci * v.y, cr * v.y + ci * v.x);
+    if (acc) {
+      double2 w = y[i];
+      w.x += p.x;
+      w.y += p.y;
+      y[i] = w;
+    } else {
+      y[i] = p;
+    }
+  }
+}
+
+// g[b] += sum_e aF[b][e] * (-mu[pol[b]][e]): dJ/dE of one RK4 stage, per
+// trajectory (F = fock - E mu_pol).  One block per trajectory, fixed-order sum.
+__global__ void __launch_bounds__(256) field_grad_kernel(const double2* __restrict__ aF, const double* __restrict__ mu,
+                                                         const int* __restrict__ pol, int nn, double2* __restrict__ g) {
+  const int b = blockIdx.x;
+  const double2* a = aF + (long long)b * nn;
+  const double* m = mu + (long long)pol[b] * nn;
+  double sr = 0.0, si = 0.0;
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+    sr -= a[e].x * m[e];
+    si -= a[e].y * m[e];
+  }
+  __shared__ double wr[8], wi[8];
+  for (int d = 16; d > 0; d >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, d);
+    si += __shfl_down_sync(0xffffffffu, si, d);
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    wr[w] = sr;
+    wi[w] = si;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tr = 0.0, ti = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      tr += wr[k];
+      ti += wi[k];
+    }
+    g[b].x += tr;
+    g[b].y += ti;
+  }
+}
+
+// a_res[b][k] = (k == pol[b]) ? w : 0  (cotangent of the recorded dipole component)
+__global__ void dipole_cotangent_kernel(double2* __restrict__ ares, const int* __restrict__ pol, int nb, int n_mu,
+                                        double w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nb * n_mu) ares[i] = make_double2((i % n_mu) == pol[i / n_mu] ? w : 0.0, 0.0);
+}
+
+static unsigned grid_for(long long n);
+
+cudaError_t launch_caxpy(double2* y, const double2* x, long long n, double cr, double ci, int acc, cudaStream_t st) {
+  caxpy_kernel<<<grid_for(n), 256, 0, st>>>(y, x, n, cr, ci, acc);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_field_grad(const double2* aF, const double* mu, const int* pol, int n, int nb, double2* g,
+                              cudaStream_t st) {
+  field_grad_kernel<<<nb, 256, 0, st>>>(aF, mu, pol, n * n, g);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dipole_cotangent(double2* ares, const int* pol, int nb, int n_mu, double w, cudaStream_t st) {
+  dipole_cotangent_kernel<<<(nb * n_mu + 127) / 128, 128, 0, st>>>(ares, pol, nb, n_mu, w);
+  count_launch();
+  return cudaGetLastError();
+}
+
 static unsigned grid_for(long long n) {
   long long b = (n + 255) / 256;
   if (b > 152 * 8) b = 152 * 8;

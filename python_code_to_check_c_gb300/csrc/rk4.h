@@ -32,6 +32,12 @@ cudaError_t launch_rk4_stage(const double2* y0, const double2* k, double2* acc, 
                              long long n, int s, double h, cudaStream_t st);
 cudaError_t launch_rk4_finish(const double2* y0, const double2* acc, double2* ynew, long long n,
                               double dt6, int sign, double scale, int do_round, cudaStream_t st);
+// reverse-mode helpers: y (+)= c x; g[b] += sum aF[b] * (-mu[pol[b]]); the
+// dipole cotangent a_res[b][k] = w * (k == pol[b])
+cudaError_t launch_caxpy(double2* y, const double2* x, long long n, double cr, double ci, int acc, cudaStream_t st);
+cudaError_t launch_field_grad(const double2* aF, const double* mu, const int* pol, int n, int nb, double2* g,
+                              cudaStream_t st);
+cudaError_t launch_dipole_cotangent(double2* ares, const int* pol, int nb, int n_mu, double w, cudaStream_t st);
 // traj[step][b] = res[b][pol[b]]; step += 1
 cudaError_t launch_record_mu(StepCtx* ctx, const double2* res, int nb, double2* traj, double* times,
                              cudaStream_t st);

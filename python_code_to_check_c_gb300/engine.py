@@ -245,6 +245,29 @@ class CCEngine:
         return tuple(st), (traj if self.nb == 1 else traj.view(int(nsteps), self.nb))
 
 
+def adjoint(eng: "CCEngine", method: str, state, t0: float, dt: float, nsteps: int, weights, field=None,
+            precs: int = -1, checkpoint: int = 50, want_state_grad: bool = False):
+    """Reverse mode through ``nsteps`` propagation steps (``tdcc_adjoint``).
+
+    J_b = sum_n weights[n] Re mu_b(t_n).  Returns (J: (nb,), gE: complex
+    (nsteps, 4, nb) -- dJ/dE at the four RK4 stage times of each step --,
+    dJ/d(initial state) conjugated, or None)."""
+    st = [to_dev(x).contiguous() for x in state]
+    w = np.ascontiguousarray(np.asarray(weights, dtype=np.float64))
+    if w.shape != (int(nsteps),):
+        raise ValueError("weights must have one entry per step")
+    J = np.zeros(eng.nb)
+    gE = np.zeros((int(nsteps), 4, eng.nb), dtype=np.complex128)
+    ast = [torch.empty_like(x) for x in st] if want_state_grad else [None] * 4
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(eng.lib.tdcc_adjoint(eng.handle, _lib.METHODS[method], *(_ptr(x) for x in st), float(t0), float(dt),
+                               int(nsteps), int(precs), ctypes.byref(field) if field is not None else None,
+                               w.ctypes.data_as(dp), int(checkpoint), J.ctypes.data_as(dp),
+                               gE.ctypes.data_as(dp), *(_ptr(x) for x in ast), _stream()),
+          "tdcc_adjoint")
+    return J, gE, (tuple(ast) if want_state_grad else None)
+
+
 def profile_step(eng: "CCEngine", method: str, state, t_prev: float, dt: float, field, precs: int = 15):
     """Per-kernel CUDA-event timings of one serial, eager RK4 step.  Returns a
     list of dicts (tag, kind, block, stage, backend, flops, bytes, ms)."""
@@ -268,4 +291,4 @@ def launch_count() -> int:
     return int(_lib.load().tdcc_launch_count())
 
 
-__all__ = ["CCEngine", "launch_count", "TDCC_CCSD", "TDCC_CC2", "TDCC_T1", "TDCC_T2", "TDCC_L1", "TDCC_L2"]
+__all__ = ["CCEngine", "adjoint", "launch_count", "TDCC_CCSD", "TDCC_CC2", "TDCC_T1", "TDCC_T2", "TDCC_L1", "TDCC_L2"]
