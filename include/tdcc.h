@@ -213,8 +213,11 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
    If a_t1..a_l2 are not NULL they receive dJ/d(initial state) (conjugated:
    conj(dJ/dRe + i dJ/dIm)).  The forward runs the captured step graphs and
    keeps the state every `checkpoint` steps; the backward recomputes each
-   segment and runs the generated reverse-mode programs (the vector-Jacobian
-   products of the right-hand sides).  The rounding of the state (precs >= 0)
+   segment on the step graphs (storing per step the state, the stage inputs
+   and the dressed Fock matrices) and runs the generated reverse-mode
+   programs (the vector-Jacobian products of the right-hand sides) stage by
+   stage.  checkpoint >= nsteps: the forward pass itself keeps every step
+   and nothing is recomputed (memory: nsteps x (4 states + Fock)).  The rounding of the state (precs >= 0)
    is taken as the identity; precs < 0 makes the map smooth.  Synchronous;
    allocates its checkpoint and segment storage for the duration of the call.
    Fields: `field` for every trajectory, or tdcc_set_fields when NULL.      */

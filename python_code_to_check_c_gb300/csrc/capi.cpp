@@ -129,6 +129,8 @@ struct tdcc_system_s {
   int g_method = -1, g_precs = -999, g_prec_mode = -1;
   double g_dt = 0.0;
   double2* g_traj = nullptr;
+  bool g_store_set = false;        // the captured graphs write per-step stores
+  StepStore g_store{};
   long long g_nodes[2] = {0, 0};   // kernel nodes per captured step graph
 
   // elements of block b for one trajectory / for all trajectories
@@ -308,7 +310,8 @@ void timed_launch(Prof* pf, cudaStream_t st, const char* tag, int block, int sta
 
 // One RK4 block (ft1/ft2/fL1/fL2): prologue once, four stages, final update.
 void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* out_b, double dt,
-               int precs, cudaStream_t st, Prof* pf = nullptr, double2* const* store = nullptr) {
+               int precs, cudaStream_t st, Prof* pf = nullptr, double2* const* store = nullptr,
+               const StepStore* ss = nullptr) {
   ProgInst& pi = get_rhs(s, method, b);
   Program& p = *pi.prog;
   auto& B = pi.bases;
@@ -333,6 +336,7 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
     // the input of stage + 1 (reverse mode recomputes each stage from it)
     if (store && stage < 4)
       CK(cudaMemcpyAsync(store[stage - 1], s->yin[b], n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    if (ss && stage < 4) CK(launch_step_store(s->ctx, s->yin[b], ss->st[b][stage - 1], ss->sst[b], n, st));
   }
   const int sign = (b == TDCC_T1 || b == TDCC_T2) ? -1 : +1;
   const double scale = precs >= 0 ? std::pow(10.0, (double)precs) : 1.0;
@@ -346,7 +350,7 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
 // runs serially on s->main.
 void run_step(tdcc_system s, int method, double2* const in[4], double2* const out[4], double dt,
               int precs, double2* traj, Prof* pf = nullptr, double2* const* store = nullptr,
-              double2* fs_store = nullptr) {
+              double2* fs_store = nullptr, const StepStore* ss = nullptr) {
   cudaStream_t m = s->main;
   const long long nn = (long long)s->dims.n * s->dims.n;
   timed_launch(pf, m, "advance_field", 5, 0, 0.0, [&] { return launch_advance_field(s->ctx, s->nb, m); });
@@ -354,13 +358,17 @@ void run_step(tdcc_system s, int method, double2* const in[4], double2* const ou
                [&] { return launch_dress(s->ctx, s->fock, s->mu, s->Fs, s->dims.n, s->nb, m); });
   if (fs_store)
     CK(cudaMemcpyAsync(fs_store, s->Fs, 3 * (size_t)s->nb * nn * sizeof(double2), cudaMemcpyDeviceToDevice, m));
+  if (ss) {
+    CK(launch_step_store(s->ctx, s->Fs, ss->fs, ss->sfs, 3 * (long long)s->nb * nn, m));
+    for (int b = 0; b < 4; ++b) CK(launch_step_store(s->ctx, in[b], ss->y[b], ss->sy[b], s->nelb(b), m));
+  }
   if (pf) {
     for (int b = 0; b < 4; ++b) run_block(s, method, b, in, out[b], dt, precs, m, pf);
   } else {
     CK(cudaEventRecord(s->ev_fork, m));
     for (int b = 0; b < 4; ++b) {
       CK(cudaStreamWaitEvent(s->bs[b], s->ev_fork, 0));
-      run_block(s, method, b, in, out[b], dt, precs, s->bs[b], nullptr, store ? store + 3 * b : nullptr);
+      run_block(s, method, b, in, out[b], dt, precs, s->bs[b], nullptr, store ? store + 3 * b : nullptr, ss);
       CK(cudaEventRecord(s->ev_join[b], s->bs[b]));
     }
     for (int b = 0; b < 4; ++b) CK(cudaStreamWaitEvent(m, s->ev_join[b], 0));
@@ -888,7 +896,7 @@ namespace {
 // (before those steps) into ck[4 * j + block].
 int propagate_impl(tdcc_system s, int method, void* t1, void* t2, void* l1, void* l2, double t0, double dt,
                    int nsteps, int precs, const tdcc_field* field, void* mu_traj, void* stream, int ck_every,
-                   double2* const* ck) {
+                   double2* const* ck, const StepStore* ss = nullptr) {
   if (!s) return fail(TDCC_ERR_ARG, "null system");
   if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
   if (!t1 || !t2 || !l1 || !l2 || !mu_traj) return fail(TDCC_ERR_ARG, "NULL argument");
@@ -906,7 +914,8 @@ int propagate_impl(tdcc_system s, int method, void* t1, void* t2, void* l1, void
     set_ctx(s, t0, dt, field, s->main);
     // (re)capture the two ping-pong step graphs when the configuration changed
     if (s->g_method != method || s->g_dt != dt || s->g_precs != precs || s->g_prec_mode != s->prec_mode ||
-        s->g_traj != mu_traj || !s->gexec[0]) {
+        s->g_traj != mu_traj || !s->gexec[0] || s->g_store_set != (ss != nullptr) ||
+        (ss && memcmp(&s->g_store, ss, sizeof(StepStore)) != 0)) {
       for (auto& g : s->gexec)
         if (g) {
           cudaGraphExecDestroy(g);
@@ -921,7 +930,7 @@ int propagate_impl(tdcc_system s, int method, void* t1, void* t2, void* l1, void
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(s->main, cudaStreamCaptureModeThreadLocal));
         try {
-          run_step(s, method, s->st[k], s->st[1 - k], dt, precs, (double2*)mu_traj);
+          run_step(s, method, s->st[k], s->st[1 - k], dt, precs, (double2*)mu_traj, nullptr, nullptr, nullptr, ss);
         } catch (...) {
           cudaStreamEndCapture(s->main, &graph);
           throw;
@@ -947,6 +956,8 @@ int propagate_impl(tdcc_system s, int method, void* t1, void* t2, void* l1, void
       s->g_precs = precs;
       s->g_prec_mode = s->prec_mode;
       s->g_traj = (double2*)mu_traj;
+      s->g_store_set = ss != nullptr;
+      if (ss) s->g_store = *ss;
     }
     // the step graphs run on the caller's stream, so its events bracket them
     CK(cudaEventRecord(s->ev_user, s->main));
@@ -1031,17 +1042,21 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
     auto nel = [&](int b) { return (size_t)s->nelb(b); };
     const size_t maxel = nel(1);
     // ---- working memory for the call ----
-    std::vector<double2*> ck(4 * nseg), y(4), segY(4 * (K + 1)), segSt(12 * K), segFs(K), ay(4), ay2(4), ak(4);
-    for (int j = 0; j < nseg; ++j)
-      for (int b = 0; b < 4; ++b) ck[4 * j + b] = alloc(nel(b) * 16);
+    // segment store: per step the state, the inputs of stages 2..4 and the
+    // dressed Fock matrices, written by the captured step graphs
+    std::vector<double2*> ck(4 * nseg), y(4), ay(4), ay2(4), ak(4);
+    if (nseg > 1)
+      for (int j = 0; j < nseg; ++j)
+        for (int b = 0; b < 4; ++b) ck[4 * j + b] = alloc(nel(b) * 16);
     for (int b = 0; b < 4; ++b) y[b] = alloc(nel(b) * 16);
-    for (int k = 0; k <= K; ++k)
-      for (int b = 0; b < 4; ++b) segY[4 * k + b] = alloc(nel(b) * 16);
-    for (int k = 0; k < K; ++k) {
-      for (int b = 0; b < 4; ++b)
-        for (int q = 0; q < 3; ++q) segSt[12 * k + 3 * b + q] = alloc(nel(b) * 16);
-      segFs[k] = alloc(3 * (size_t)nb * nn * 16);
+    StepStore ss{};
+    for (int b = 0; b < 4; ++b) {
+      ss.sy[b] = ss.sst[b] = (long long)nel(b);
+      ss.y[b] = alloc((size_t)K * nel(b) * 16);
+      for (int q = 0; q < 3; ++q) ss.st[b][q] = alloc((size_t)K * nel(b) * 16);
     }
+    ss.sfs = 3LL * nb * nn;
+    ss.fs = alloc((size_t)K * ss.sfs * 16);
     for (int b = 0; b < 4; ++b) {
       ay[b] = alloc(nel(b) * 16);
       ay2[b] = alloc(nel(b) * 16);
@@ -1053,14 +1068,18 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
     double2* ares = alloc((size_t)nb * n_mu * 16);
     double2* gE = alloc((size_t)nsteps * 4 * nb * 16);
     double2* traj = alloc((size_t)nsteps * nb * 16);
+    double2* straj = alloc((size_t)K * nb * 16);
     CK(cudaMemsetAsync(gE, 0, (size_t)nsteps * 4 * nb * 16, m));
     const void* in[4] = {t1, t2, l1, l2};
     for (int b = 0; b < 4; ++b) CK(cudaMemcpyAsync(y[b], in[b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
     CK(cudaStreamSynchronize(m));
 
-    // ---- forward: the captured step graphs, checkpoints every K steps ----
-    const int rc = propagate_impl(s, method, y[0], y[1], y[2], y[3], t0, dt, nsteps, precs, field, traj, m, K,
-                                  ck.data());
+    // ---- forward on the captured step graphs: one segment keeps every step,
+    //      otherwise checkpoints every K steps ----
+    const int rc = nseg == 1 ? propagate_impl(s, method, y[0], y[1], y[2], y[3], t0, dt, nsteps, precs, field, traj, m,
+                                              1, nullptr, &ss)
+                             : propagate_impl(s, method, y[0], y[1], y[2], y[3], t0, dt, nsteps, precs, field, traj, m,
+                                              K, ck.data());
     if (rc != TDCC_OK) return rc;
     {
       std::vector<double2> ht((size_t)nsteps * nb);
@@ -1079,14 +1098,18 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
     const double hst[4] = {0.0, dt / 2.0, dt / 2.0, dt};  // Y(s) = y + h_s k_(s-1)
     for (int j = nseg - 1; j >= 0; --j) {
       const int k0 = j * K, kn = std::min(K, nsteps - k0);
-      double tk = t0;
-      for (int i = 0; i < k0; ++i) tk += dt;  // the forward's time accumulation
-      for (int b = 0; b < 4; ++b)
-        CK(cudaMemcpyAsync(segY[b], ck[4 * j + b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
-      set_ctx(s, tk, dt, field, m);
-      for (int k = 0; k < kn; ++k)
-        run_step(s, method, &segY[4 * k], &segY[4 * (k + 1)], dt, precs, nullptr, nullptr, &segSt[12 * k],
-                 segFs[k]);
+      if (nseg > 1) {
+        // recompute the segment on the step graphs, filling the store; y ends
+        // as the state after the segment
+        double tk = t0;
+        for (int i = 0; i < k0; ++i) tk += dt;  // the forward's time accumulation
+        for (int b = 0; b < 4; ++b)
+          CK(cudaMemcpyAsync(y[b], ck[4 * j + b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
+        const int rs = propagate_impl(s, method, y[0], y[1], y[2], y[3], tk, dt, kn, precs, field, straj, m, 1,
+                                      nullptr, &ss);
+        if (rs != TDCC_OK) return rs;
+      }
+      auto yk = [&](int k, int b) { return k < kn ? ss.y[b] + (size_t)k * ss.sy[b] : y[b]; };
       for (int k = kn - 1; k >= 0; --k) {
         const int nstep = k0 + k;
         // the objective's dipole term at y_(n+1)
@@ -1094,7 +1117,7 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
           ProgInst& d = get_density(s);
           ProgInst& ad = get_adj(s, method, 4);
           const auto& aof = s->adj_of[method][4];
-          for (int q = 0; q < 4; ++q) d.bases[S_T1 + q] = segY[4 * (k + 1) + q];
+          for (int q = 0; q < 4; ++q) d.bases[S_T1 + q] = yk(k + 1, q);
           d.bases[S_RES] = s->res;
           CK(d.exec(m, Program::ALL));
           for (size_t i = 0; i < ad.nfwd; ++i) ad.bases[i] = d.bases[i];
@@ -1106,21 +1129,22 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
         }
         // step adjoint: ay (of y_(n+1)) -> ay2 (of y_n); rounding taken as the identity
         for (int q = 0; q < 4; ++q) CK(cudaMemcpyAsync(ay2[q], ay[q], nel(q) * 16, cudaMemcpyDeviceToDevice, m));
+        double2* Fk = ss.fs + (size_t)k * ss.sfs;
         for (int b = 0; b < 4; ++b) {
           ProgInst& pi = get_rhs(s, method, b);
           ProgInst& ai = get_adj(s, method, b);
           const auto& aof = s->adj_of[method][b];
           auto& B = pi.bases;
-          for (int q = 0; q < 4; ++q) B[S_T1 + q] = segY[4 * k + q];
+          for (int q = 0; q < 4; ++q) B[S_T1 + q] = yk(k, q);
           B[S_OUT] = s->kbuf[b];
-          B[S_F] = segFs[k];
+          B[S_F] = Fk;
           CK(pi.exec(m, Program::PROLOGUE));
           // a_k(s) = c w_s a_out, c = -i dt/6 (T) or +i dt/6 (Lambda)
           const double ci = (b == TDCC_T1 || b == TDCC_T2) ? -c6 : c6;
           for (int st = 0; st < 4; ++st) CK(launch_caxpy(ak[st], ay[b], nel(b), 0.0, wst[st] * ci, 0, m));
           for (int st = 4; st >= 1; --st) {
-            B[S_T1 + b] = st == 1 ? segY[4 * k + b] : segSt[12 * k + 3 * b + (st - 2)];
-            B[S_F] = segFs[k] + (size_t)(st == 1 ? 0 : st < 4 ? 1 : 2) * nb * nn;
+            B[S_T1 + b] = st == 1 ? yk(k, b) : ss.st[b][st - 2] + (size_t)k * ss.sst[b];
+            B[S_F] = Fk + (size_t)(st == 1 ? 0 : st < 4 ? 1 : 2) * nb * nn;
             CK(pi.exec(m, Program::STAGE));
             for (size_t i = 0; i < ai.nfwd; ++i) ai.bases[i] = B[i];
             CK(cudaMemcpyAsync(akin, ak[st - 1], nel(b) * 16, cudaMemcpyDeviceToDevice, m));

@@ -193,7 +193,21 @@ __global__ void dipole_cotangent_kernel(double2* __restrict__ ares, const int* _
   if (i < nb * n_mu) ares[i] = make_double2((i % n_mu) == pol[i / n_mu] ? w : 0.0, 0.0);
 }
 
+__global__ void step_store_kernel(const StepCtx* ctx, const double2* __restrict__ src, double2* __restrict__ dst,
+                                  long long stride, long long n) {
+  double2* d = dst + ctx->step * stride;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    d[i] = src[i];
+}
+
 static unsigned grid_for(long long n);
+
+cudaError_t launch_step_store(const StepCtx* ctx, const double2* src, double2* dst_base, long long stride, long long n,
+                              cudaStream_t st) {
+  step_store_kernel<<<grid_for(n), 256, 0, st>>>(ctx, src, dst_base, stride, n);
+  count_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t launch_caxpy(double2* y, const double2* x, long long n, double cr, double ci, int acc, cudaStream_t st) {
   caxpy_kernel<<<grid_for(n), 256, 0, st>>>(y, x, n, cr, ci, acc);

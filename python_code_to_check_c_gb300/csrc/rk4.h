@@ -24,6 +24,23 @@ struct StepCtx {
 
 constexpr int kMaxTrajectories = 1024;
 
+// Per-step stores for reverse mode, written inside the captured step graph:
+// step k's state goes to y[b] + k * sy[b], the inputs of its stages 2..4 to
+// st[b][q] + k * sst[b], its dressed Fock matrices to fs + k * sfs (k is the
+// device step counter).
+struct StepStore {
+  double2* y[4];
+  long long sy[4];
+  double2* st[4][3];
+  long long sst[4];
+  double2* fs;
+  long long sfs;
+};
+
+// dst_base + ctx->step * stride  <-  src  (n elements)
+cudaError_t launch_step_store(const StepCtx* ctx, const double2* src, double2* dst_base, long long stride, long long n,
+                              cudaStream_t st);
+
 cudaError_t launch_advance_field(StepCtx* ctx, int nb, cudaStream_t st);
 // Fs[s][b] = fock - E[b][s] * mu[pol[b]]  (stage-major: [3][nb][n][n])
 cudaError_t launch_dress(const StepCtx* ctx, const double* fock, const double* mu, double2* Fs, int n,

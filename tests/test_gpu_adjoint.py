@@ -18,8 +18,10 @@ def _J(eng, method, st, pulse, t0, dt, n, w):
     return float(np.sum(w * traj.detach().cpu().numpy().real))
 
 
-@pytest.mark.parametrize("method", ["CCSD", "CC2"])
-def test_pulse_gradient_matches_finite_differences(method):
+@pytest.mark.parametrize("method,checkpoint", [("CCSD", 5), ("CC2", 5), ("CCSD", 1000)])
+def test_pulse_gradient_matches_finite_differences(method, checkpoint):
+    """checkpoint 5: segments recomputed from checkpoints; 1000 >= the step
+    count: every step kept by the forward pass."""
     from python_code_to_check_c_gb300.engine import CCEngine
     from python_code_to_check_c_gb300.pulse import Pulse, cosine_weights, pulse_gradient
     d, sysm = load("golden_o4_v8.npz")
@@ -31,7 +33,7 @@ def test_pulse_gradient_matches_finite_differences(method):
     w = cosine_weights(t0, dt, n)
     eng = CCEngine.from_system(sysm)
     try:
-        J, gA, gw, gc = pulse_gradient(eng, method, st, pulse, t0, dt, n, w, checkpoint=5)
+        J, gA, gw, gc = pulse_gradient(eng, method, st, pulse, t0, dt, n, w, checkpoint=checkpoint)
         assert abs(J - _J(eng, method, st, pulse, t0, dt, n, w)) < 1e-13
         fd = []
         for name in ["A", "w0"] + [f"c{k}" for k in range(len(pulse.c))]:
