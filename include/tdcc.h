@@ -227,6 +227,18 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
                  double* J_out, double* gE_host, void* a_t1, void* a_t2, void* a_l1,
                  void* a_l2, void* stream);
 
+/* Autotuner (no counterpart in the reference): runs one step from the given
+   state to fill the workspaces, then times every contraction of the
+   method's programs under candidate launch shapes -- FP64 kernel: tile shape
+   x split-K on/off; tensor-core kernel: K splits -- and keeps the fastest
+   (reps timed launches each, CUDA events).  Recomputes the per-system
+   constants afterwards and drops the captured step graphs.  n_tuned: ops
+   changed; ms_before / ms_after: summed per-launch times of all
+   contractions (one pass of every op).  Any pointer output may be NULL.   */
+int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, const void* l1,
+                  const void* l2, int reps, int* n_tuned, double* ms_before, double* ms_after,
+                  void* stream);
+
 /* Reverse-mode op list of (method, block) as JSON (like tdcc_program_json):
    forward slots [0, nfwd), adjoint slots after them, "adj_of" maps each
    forward slot to its adjoint slot (-1: not differentiable).  No GPU.     */

@@ -75,6 +75,8 @@ SIGNATURES = {
                            ctypes.POINTER(TdccField), _vp, _vp]),
     "tdcc_propagate": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _d, _i, _i,
                             ctypes.POINTER(TdccField), _vp, _vp]),
+    "tdcc_autotune": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_d),
+                           ctypes.POINTER(_d), _vp]),
     "tdcc_adjoint": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _d, _i, _i, ctypes.POINTER(TdccField),
                           ctypes.POINTER(_d), _i, ctypes.POINTER(_d), ctypes.POINTER(_d), _vp, _vp, _vp, _vp, _vp]),
     "tdcc_dipole_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp]),

@@ -100,6 +100,8 @@ struct tdcc_system_s {
   int tc_min_k = kTcMinK;
   int device = 0;
   int nb = 1;                       // trajectories advanced together
+  bool share_mem = true;            // workspace slots with disjoint lifetimes share memory (off once
+                                    // reverse mode is used: it reads every forward value after a stage)
   std::vector<tdcc_field> h_fields; // per-trajectory fields (tdcc_set_fields)
   std::vector<int> h_pol;
   std::unique_ptr<ProgInst> rhs[2][4];
@@ -193,6 +195,7 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
   p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
+  if (s->share_mem) p.plan_memory();
   pi->bases.assign(p.slots.size(), nullptr);
   pi->bytes = p.allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;
@@ -210,6 +213,7 @@ ProgInst& get_density(tdcc_system s) {
   pi->prog->batch(s->nb);
   pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   pi->prog->analyse({});
+  if (s->share_mem) pi->prog->plan_memory();
   pi->bases.assign(pi->prog->slots.size(), nullptr);
   pi->bytes = pi->prog->allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;
@@ -220,12 +224,17 @@ ProgInst& get_density(tdcc_system s) {
 }
 
 void build_program(Program& p, int method, int block, int n_mu, int nb);
+void reset_programs(tdcc_system s);
 
 // Reverse-mode program of (method, block); block 4 = density.  Its slots
 // [0, nfwd) are bound to the forward instance's buffers before every run.
 ProgInst& get_adj(tdcc_system s, int method, int block) {
   auto& slot = s->adjp[method][block];
   if (slot) return *slot;
+  if (s->share_mem) {  // rebuild the forward programs with a buffer per slot
+    reset_programs(s);
+    s->share_mem = false;
+  }
   if (block == 4)
     get_density(s);
   else
@@ -999,6 +1008,119 @@ int tdcc_propagate(tdcc_system s, int method, void* t1, void* t2, void* l1, void
   return propagate_impl(s, method, t1, t2, l1, l2, t0, dt, nsteps, precs, field, mu_traj, stream, 1, nullptr);
 }
 
+int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, const void* l1, const void* l2,
+                  int reps, int* n_tuned, double* ms_before, double* ms_after, void* stream) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (!valid_method(method)) return fail(TDCC_ERR_ARG, "bad method");
+  if (!t1 || !t2 || !l1 || !l2) return fail(TDCC_ERR_ARG, "NULL state pointer");
+  if (reps < 1) reps = 3;
+  int tuned = 0;
+  double before = 0.0, after = 0.0;
+  try {
+    ensure_rk(s);
+    cudaStream_t user = static_cast<cudaStream_t>(stream), m = s->main;
+    CK(cudaEventRecord(s->ev_user, user));
+    CK(cudaStreamWaitEvent(m, s->ev_user, 0));
+    // one eager step fills every workspace with realistic values
+    tdcc_field none;
+    memset(&none, 0, sizeof(none));
+    none.kind = TDCC_FIELD_NONE;
+    set_ctx(s, 0.0, 1e-3, &none, m);
+    double2* in[4] = {(double2*)t1, (double2*)t2, (double2*)l1, (double2*)l2};
+    double2* tmp[4] = {s->st[1][0], s->st[1][1], s->st[1][2], s->st[1][3]};
+    run_step(s, method, in, tmp, 1e-3, -1, nullptr);
+    CK(cudaStreamSynchronize(m));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto time_op = [&](ProgInst& pi, const Op& op) {
+      CK(pi.prog->launch_op(op, pi.bases, m));  // warm
+      CK(cudaEventRecord(e0, m));
+      for (int r = 0; r < reps; ++r) CK(pi.prog->launch_op(op, pi.bases, m));
+      CK(cudaEventRecord(e1, m));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      return (double)ms / reps;
+    };
+    std::vector<ProgInst*> progs;
+    for (int b = 0; b < 4; ++b) progs.push_back(&get_rhs(s, method, b));
+    progs.push_back(&get_density(s));
+    for (ProgInst* pip : progs) {
+      ProgInst& pi = *pip;
+      pi.check_bound();
+      for (Op& op : pi.prog->ops) {
+        if (op.kind == OP_GEMM) {
+          const double t_cur = time_op(pi, op);
+          double best = t_cur;
+          Op best_op = op;
+          for (int tile = 0; tile < kNumTiles; ++tile)
+            for (int split = 0; split < 2; ++split) {
+              Op c = op;
+              Program::plan_gemm(c, split == 1 && op.zeroed, tile);
+              if (c.tile == op.tile && c.g.nsplit == op.g.nsplit) continue;
+              const double t = time_op(pi, c);
+              if (t < best * 0.97) {
+                best = t;
+                best_op = c;
+              }
+            }
+          before += t_cur;
+          after += best;
+          if (best_op.tile != op.tile || best_op.g.nsplit != op.g.nsplit) {
+            op = best_op;
+            ++tuned;
+          }
+        } else if (op.kind == OP_TCGEMM) {
+          const double t_cur = time_op(pi, op);
+          double best = t_cur;
+          TcArgs best_a = op.tc;
+          if (op.zeroed)
+            for (int sp : {1, 2, 3, 4, 6, 8, 12, 16}) {
+              if (sp > op.tc.kblocks) break;
+              Op c = op;
+              c.tc.kb_per_split = (c.tc.kblocks + sp - 1) / sp;
+              c.tc.nsplit = (c.tc.kblocks + c.tc.kb_per_split - 1) / c.tc.kb_per_split;
+              c.tc.atomic = c.tc.nsplit > 1 ? 1 : 0;
+              if (c.tc.nsplit == op.tc.nsplit) continue;
+              if (!c.tc.atomic && !c.tc.acc) continue;  // plain store needs one writer per element
+              const double t = time_op(pi, c);
+              if (t < best * 0.97) {
+                best = t;
+                best_a = c.tc;
+              }
+            }
+          before += t_cur;
+          after += best;
+          if (best_a.nsplit != op.tc.nsplit) {
+            op.tc = best_a;
+            ++tuned;
+          }
+        }
+      }
+      // tuned ops ran on live workspaces: recompute the per-system constants
+      pi.setup_done = false;
+      CK(pi.setup(m));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (auto& g : s->gexec)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    CK(cudaStreamSynchronize(m));
+    CK(cudaEventRecord(s->ev_user, m));
+    CK(cudaStreamWaitEvent(user, s->ev_user, 0));
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  if (n_tuned) *n_tuned = tuned;
+  if (ms_before) *ms_before = before;
+  if (ms_after) *ms_after = after;
+  return TDCC_OK;
+}
+
 int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, const void* l1, const void* l2,
                  double t0, double dt, int nsteps, int precs, const tdcc_field* field, const double* w_host,
                  int checkpoint, double* J_out, double* gE_host, void* a_t1, void* a_t2, void* a_l1, void* a_l2,
@@ -1257,6 +1379,7 @@ void build_program(Program& p, int method, int block, int n_mu, int nb = 1) {
     p.analyse({});
   else
     p.analyse({S_T1 + block, S_F});
+  p.plan_memory();  // introspection shows the buffer sharing the runtime uses
 }
 
 std::string jarr(const long long* x, int n) {
@@ -1285,6 +1408,7 @@ std::string program_json(const Program& p) {
     const auto& s = p.slots[i];
     j += (i ? "," : "") + std::string("{\"name\":\"") + s.name + "\",\"dt\":" + std::to_string(s.dt) +
          ",\"numel\":" + std::to_string(s.numel) + ",\"numel1\":" + std::to_string(s.numel1) +
+         ",\"buf\":" + std::to_string(i < p.slot_buf.size() ? p.slot_buf[i] : (int)i) +
          ",\"batched\":" + (s.batched ? "true" : "false") + ",\"fixed\":" + (s.fixed ? "true" : "false") +
          ",\"ones\":" + (s.init.empty() ? "false" : "true") + "}";
   }

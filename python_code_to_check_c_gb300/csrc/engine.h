@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -295,8 +296,15 @@ class Program {
   int nb = 1;
   long long bstride(int slot) const { return slots[slot].batched ? slots[slot].numel1 : 0; }
   // tile shape and split-K of a contraction from its extents
-  static void plan_gemm(Op& op, bool allow_split);
+  static void plan_gemm(Op& op, bool allow_split, int tile = -1);
 
+  // shares memory between workspace slots with disjoint lifetimes within one
+  // phase (after analyse; before allocate); without it every slot is its own
+  void plan_memory(size_t first = 0);
+  std::vector<int> slot_buf;              // buffer (representative slot) of each slot
+  std::map<int, int> pool_of;             // slot -> shared buffer index
+  std::vector<int> buf_slot;              // shared buffer -> its first slot
+  std::vector<size_t> pool_bytes;
   // device allocation of the non-fixed slots from index `first` on (returns
   // bytes allocated); `zero`: clear them (accumulators of adjoint programs)
   long long allocate(std::vector<void*>& bases, std::vector<void*>& owned, size_t first = 0, bool zero = false);

@@ -255,10 +255,10 @@ void Program::ein(const char* spec, double ar, double ai, const View& A, const V
 // Tile shape, then split-K so that few output tiles still fill the 152 SMs
 // (only where the output is zeroed or accumulated into: splits add with
 // atomics).
-void Program::plan_gemm(Op& op, bool allow_split) {
+void Program::plan_gemm(Op& op, bool allow_split, int tile) {
   GemmArgs& g = op.g;
   const long long M = g.M, N = g.N, K = g.K, nbt = std::max(g.nb, 1);
-  op.tile = choose_tile(M, N);
+  op.tile = tile >= 0 ? tile : choose_tile(M, N);
   const long long tiles = ((M + kTiles[op.tile][0] - 1) / kTiles[op.tile][0]) *
                           ((N + kTiles[op.tile][1] - 1) / kTiles[op.tile][1]) * nbt;
   long long splits = 1;
@@ -577,11 +577,100 @@ void Program::batch(int nbt) {
   }
 }
 
+// Buffer sharing: a workspace slot touched only by ops of one phase (setup,
+// prologue or stage), defined before it is read, can share memory with any
+// other such slot whose program-order lifetime [first op, last op] does not
+// overlap.  Every way a program is executed (whole, dynamic part, prologue
+// then stages) keeps program order within a phase, and the DAG executor
+// orders accesses by buffer, so the shared memory is never live twice.
+void Program::plan_memory(size_t first) {
+  slot_buf.resize(slots.size());
+  for (size_t i = 0; i < slots.size(); ++i) slot_buf[i] = (int)i;
+  const size_t n = slots.size();
+  std::vector<int> f(n, -1), l(n, -1), ph(n, -1);
+  std::vector<char> mixed(n, 0), read_first(n, 0);
+  for (size_t k = 0; k < ops.size(); ++k) {
+    const Op& op = ops[k];
+    const int p = op.is_const ? 0 : op.varying ? 2 : 1;
+    auto touch = [&](int sl, bool is_write) {
+      if (sl < 0) return;
+      if (f[sl] < 0) {
+        f[sl] = (int)k;
+        if (!is_write) read_first[sl] = 1;
+      }
+      l[sl] = (int)k;
+      if (ph[sl] < 0) ph[sl] = p;
+      else if (ph[sl] != p) mixed[sl] = 1;
+    };
+    for (int r : op.reads) touch(r, false);
+    if (op.write >= 0) {
+      // an op that reads its own output (accumulate) reads before writing
+      bool reads_self = false;
+      for (int r : op.reads) reads_self |= r == op.write;
+      touch(op.write, !reads_self);
+    }
+  }
+  struct Buf {
+    size_t bytes;
+    int free_after;  // last op index of its current occupant
+  };
+  std::vector<Buf> pool;
+  std::vector<int> order;
+  for (size_t i = std::max<size_t>(first, kNumFixedSlots); i < n; ++i) {
+    if (slots[i].fixed || !slots[i].init.empty() || (int)i == err_slot || f[i] < 0 || mixed[i] || read_first[i] ||
+        ph[i] == 0)
+      continue;
+    order.push_back((int)i);
+  }
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return f[a] < f[b]; });
+  for (int sl : order) {
+    const size_t bytes = (size_t)slots[sl].numel * (size_t)elem_bytes(slots[sl].dt);
+    int best = -1;
+    for (size_t q = 0; q < pool.size(); ++q)
+      if (pool[q].free_after < f[sl] && pool[q].bytes >= bytes && (best < 0 || pool[q].bytes < pool[best].bytes))
+        best = (int)q;
+    if (best < 0)
+      for (size_t q = 0; q < pool.size(); ++q)  // grow the largest free buffer
+        if (pool[q].free_after < f[sl] && (best < 0 || pool[q].bytes > pool[best].bytes)) best = (int)q;
+    if (best < 0) {
+      pool.push_back({bytes, l[sl]});
+      buf_slot.push_back(sl);
+      slot_buf[sl] = sl;
+      pool_of[sl] = (int)pool.size() - 1;
+    } else {
+      pool[best].bytes = std::max(pool[best].bytes, bytes);
+      pool[best].free_after = l[sl];
+      slot_buf[sl] = buf_slot[best];
+      pool_of[sl] = best;
+    }
+  }
+  pool_bytes.clear();
+  for (const auto& b : pool) pool_bytes.push_back(b.bytes);
+}
+
 long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned, size_t first, bool zero) {
   long long bytes = 0;
   if (bases.size() < slots.size()) bases.resize(slots.size(), nullptr);
+  // shared buffers first (plan_memory), then every other slot
+  std::vector<void*> pool_ptr(pool_bytes.size(), nullptr);
+  for (size_t q = 0; q < pool_bytes.size(); ++q) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, pool_bytes[q]) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::runtime_error("cudaMalloc failed for a shared workspace buffer in " + name);
+    }
+    owned.push_back(p);
+    pool_ptr[q] = p;
+    if (zero && cudaMemset(p, 0, pool_bytes[q]) != cudaSuccess) throw std::runtime_error("zeroing workspace failed");
+    bytes += (long long)pool_bytes[q];
+  }
   for (size_t i = std::max<size_t>(first, kNumFixedSlots); i < slots.size(); ++i) {
     if (slots[i].fixed) continue;
+    auto it = pool_of.find((int)i);
+    if (it != pool_of.end()) {
+      bases[i] = pool_ptr[it->second];
+      continue;
+    }
     const size_t b = (size_t)slots[i].numel * (size_t)elem_bytes(slots[i].dt);
     void* p = nullptr;
     if (cudaMalloc(&p, b) != cudaSuccess) {
@@ -720,6 +809,8 @@ cudaError_t Program::run_dag(const std::vector<void*>& bases, cudaStream_t st, P
                              DagExec& ex) const {
   ex.init(ops.size(), 4);
   const int ns = (int)ex.streams.size();
+  // hazards are tracked per buffer: slots that share memory are ordered too
+  auto buf = [&](int sl) { return (sl >= 0 && sl < (int)slot_buf.size()) ? slot_buf[sl] : sl; };
   std::vector<int> last_writer(slots.size(), -1);
   std::vector<std::vector<int>> readers(slots.size());
   std::vector<int> op_stream(ops.size(), -1);
@@ -733,10 +824,10 @@ cudaError_t Program::run_dag(const std::vector<void*>& bases, cudaStream_t st, P
     if (!in_phase(op, ph)) continue;
     std::vector<int> deps;
     for (int r : op.reads)
-      if (r >= 0 && last_writer[r] >= 0) deps.push_back(last_writer[r]);
+      if (r >= 0 && last_writer[buf(r)] >= 0) deps.push_back(last_writer[buf(r)]);
     if (op.write >= 0) {
-      if (last_writer[op.write] >= 0) deps.push_back(last_writer[op.write]);
-      for (int rd : readers[op.write]) deps.push_back(rd);
+      if (last_writer[buf(op.write)] >= 0) deps.push_back(last_writer[buf(op.write)]);
+      for (int rd : readers[buf(op.write)]) deps.push_back(rd);
     }
     std::sort(deps.begin(), deps.end());
     deps.erase(std::unique(deps.begin(), deps.end()), deps.end());
@@ -764,10 +855,10 @@ cudaError_t Program::run_dag(const std::vector<void*>& bases, cudaStream_t st, P
     op_stream[i] = s;
     tail[s] = (int)i;
     for (int r : op.reads)
-      if (r >= 0) readers[r].push_back((int)i);
+      if (r >= 0) readers[buf(r)].push_back((int)i);
     if (op.write >= 0) {
-      last_writer[op.write] = (int)i;
-      readers[op.write].clear();
+      last_writer[buf(op.write)] = (int)i;
+      readers[buf(op.write)].clear();
     }
   }
   // join every used stream back into the caller's stream
@@ -979,6 +1070,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     splits = (a.kblocks + a.kb_per_split - 1) / a.kb_per_split;
     a.nsplit = (int)splits;
     a.atomic = splits > 1 ? 1 : 0;
+    t.zeroed = a.acc || a.atomic;  // split K is allowed (a zero op precedes when not accumulating)
     t.bytes = (long long)S * (nbA * rA + nbB * rB) * Kp * 2 + nbt * M * N * elem_bytes(op.dtc);
     t.reads = {pa.pk_dst, pb.pk_dst};
     if (a.acc || a.atomic) t.reads.push_back(op.sc);

@@ -121,6 +121,19 @@ class CCEngine:
         """Which contractions the mixed mode sends to the tensor cores."""
         check(self.lib.tdcc_set_tc_policy(self.handle, int(min_macs), int(min_k)), "tdcc_set_tc_policy")
 
+    def autotune(self, method: str, state, reps: int = 3):
+        """Picks the launch shape of every contraction by timing candidates
+        on this system (``tdcc_autotune``); returns (ops changed, summed
+        contraction ms before, after)."""
+        st = [to_dev(x) for x in state]
+        n = ctypes.c_int(0)
+        b = ctypes.c_double(0.0)
+        a = ctypes.c_double(0.0)
+        check(self.lib.tdcc_autotune(self.handle, _lib.METHODS[method], *(_ptr(x) for x in st), int(reps),
+                                     ctypes.byref(n), ctypes.byref(b), ctypes.byref(a), _stream()),
+              "tdcc_autotune")
+        return n.value, b.value, a.value
+
     def check_errors(self):
         """Synchronises and raises if a kernel recorded an error (an expired
         bounded wait in a tensor-core kernel)."""

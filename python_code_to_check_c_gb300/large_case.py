@@ -1,0 +1,96 @@
+"""Large TD-CCSD / TD-CC2 on one GPU:
+    python -m python_code_to_check_c_gb300.large_case [--workload o24_v160] [--method CCSD]
+        [--mixed-steps 10] [--fp64-steps 2]
+
+Seeded DF integrals (Q = 480 at o=24, v=160), MP2-guess start (t1 = 0,
+t2 = MP2, lambda = t: a ground-state solve at this size costs more than the
+measurement and does not change the cost of a step), dt = 0.005,
+E = 0.002 sin(0.923 t).  Prints one JSON line: steps/s of the mixed and FP64
+forms (captured step graphs, CUDA events), |d mu| between them over the FP64
+steps, and per-contraction rates of one mixed step from CUDA events around
+every launch (the ladder and ring contractions with their tensor work
+fraction: FP64-equivalent flops x slice products / time / measured BF16 peak)."""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+import numpy as np
+import torch
+
+from ._lib import make_field
+from .engine import CCEngine, profile_step
+from .system import WORKLOADS, mp2_guess, synthetic_system
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--workload", default="o24_v160")
+    p.add_argument("--method", default="CCSD")
+    p.add_argument("--mixed-steps", type=int, default=10)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    a = p.parse_args()
+    t_build = time.perf_counter()
+    sysm = synthetic_system(**WORKLOADS[a.workload])
+    tei = sysm.tei()
+    eng = CCEngine(tei, sysm.fock, sysm.mu, sysm.o)
+    t2 = mp2_guess(tei, sysm.eps(), sysm.o).astype(np.complex128)
+    del tei
+    t1 = np.zeros((sysm.o, sysm.v), dtype=np.complex128)
+    st = [torch.as_tensor(x, device="cuda") for x in (t1, t2, t1.copy(), t2.copy())]
+    build_s = time.perf_counter() - t_build
+    f = make_field("sin", 0.002, 0.923)
+
+    def timed(steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _, traj = eng.propagate(a.method, st, 0.0, 0.005, steps, f)
+        e1.record()
+        torch.cuda.synchronize()
+        return traj, e0.elapsed_time(e1) / 1e3
+
+    eng.set_precision("mixed", 5)
+    eng.propagate(a.method, st, 0.0, 0.005, 1, f)
+    trmx, smx = timed(a.mixed_steps)
+    eng.check_errors()
+    recs = profile_step(eng, a.method, st, 0.0, 0.005, f)
+    ws_mixed = eng.workspace_bytes()
+    eng.set_precision("fp64")
+    eng.propagate(a.method, st, 0.0, 0.005, 1, f)
+    tr64, s64 = timed(a.fp64_steps)
+    k = min(a.fp64_steps, a.mixed_steps)
+    dmu = float((trmx[:k] - tr64[:k]).abs().max().item())
+    peak = 1886.4
+    try:
+        peak = json.load(open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                           "MEASURED_PEAKS.json")))["bf16_tflops"]
+    except Exception:
+        pass
+    agg = {}
+    for r in recs:
+        if r["kind"] != 0:
+            continue
+        x = agg.setdefault((r["tag"], r["backend"]), [0.0, 0.0, 0])
+        x[0] += r["ms"]
+        x[1] += r["flops"]
+        x[2] += 1
+    tot = sum(r["ms"] for r in recs)
+    top = sorted(agg.items(), key=lambda kv: -kv[1][0])[:8]
+    contractions = [{"op": tag, "tensor_cores": bool(be), "launches": n, "share_of_step": ms / tot,
+                     "fp64_equiv_tflops": fl / (ms / 1e3) / 1e12,
+                     "tensor_work_frac": (fl * 15 / (ms / 1e3) / 1e12 / peak) if be else None}
+                    for (tag, be), (ms, fl, n) in top]
+    print(json.dumps({
+        "workload": a.workload, "method": a.method, "o": sysm.o, "v": sysm.v, "nq": sysm.nq,
+        "build_s": build_s, "mixed_steps_per_s": a.mixed_steps / smx, "mixed_steps": a.mixed_steps,
+        "fp64_steps_per_s": a.fp64_steps / s64, "fp64_steps": a.fp64_steps,
+        "mixed_over_fp64": (a.mixed_steps / smx) / (a.fp64_steps / s64), "max_dmu_au": dmu, "dmu_steps": k,
+        "workspace_gb_mixed": ws_mixed / 1e9, "serial_step_ms_mixed": tot, "top_contractions": contractions}))
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -20,16 +20,31 @@ def _group(g):
 
 
 class Emulator:
-    def __init__(self, prog, o, v, n_mu=3):
+    """``share``: workspace slots the program maps to one buffer ("buf") alias
+    the same memory, as on the device (off for reverse-mode checks, which
+    read every forward value after the forward ran -- the runtime turns the
+    sharing off for them too)."""
+
+    def __init__(self, prog, o, v, n_mu=3, share=True):
         self.p = prog
         self.o, self.v, self.n = o, v, o + v
         self.n_mu = n_mu
         self.bufs = {}
+        groups = {}
         for i, s in enumerate(prog["slots"]):
             if s["fixed"]:
                 continue
-            dt = np.complex128 if s["dt"] == 1 else np.float64
-            self.bufs[i] = np.ones(s["numel"], dtype=dt) if s["ones"] else np.zeros(s["numel"], dtype=dt)
+            b = s.get("buf", i) if share else i
+            size = {0: 8, 1: 16, 2: 1}[s["dt"]] * s["numel"]
+            groups.setdefault(b, []).append((i, s, size))
+        for b, members in groups.items():
+            raw = bytearray(max(sz for _, _, sz in members))
+            for i, s, _ in members:
+                dt = {0: np.float64, 1: np.complex128, 2: np.uint8}[s["dt"]]
+                arr = np.frombuffer(raw, dtype=dt, count=s["numel"])
+                if s["ones"]:
+                    arr[:] = 1
+                self.bufs[i] = arr
 
     def bind(self, slot, arr):
         self.bufs[slot] = np.ascontiguousarray(arr).reshape(-1)

@@ -35,7 +35,7 @@ def _forward(sysm, tei, method, block, x, nb):
     from python_code_to_check_c_gb300._lib import program_json
     o, v = sysm.o, sysm.v
     prog = program_json(o, v, method, block, 3, nb)
-    e = Emulator(prog, o, v)
+    e = Emulator(prog, o, v, share=False)
     e.bind(S_TEI, tei)
     e.bind(S_MU, np.stack(sysm.mu))
     for s in INPUTS:
@@ -186,7 +186,7 @@ def test_adjoint_phase_split(small, method, block):
     # phased run
     fwd = program_json(o, v, method, block, 3, 1)
     adj = adjoint_program_json(o, v, method, block, 3, 1)
-    ef = Emulator(fwd, o, v)
+    ef = Emulator(fwd, o, v, share=False)
     ef.bind(S_TEI, tei)
     ef.bind(S_MU, np.stack(sysm.mu))
     for s in INPUTS:
