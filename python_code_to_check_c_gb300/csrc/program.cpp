@@ -661,7 +661,8 @@ long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned
     }
     owned.push_back(p);
     pool_ptr[q] = p;
-    if (zero && cudaMemset(p, 0, pool_bytes[q]) != cudaSuccess) throw std::runtime_error("zeroing workspace failed");
+    // all-ones bytes are NaN: a read of memory no op wrote cannot pass silently
+    if (cudaMemset(p, zero ? 0 : 0xFF, pool_bytes[q]) != cudaSuccess) throw std::runtime_error("clearing workspace failed");
     bytes += (long long)pool_bytes[q];
   }
   for (size_t i = std::max<size_t>(first, kNumFixedSlots); i < slots.size(); ++i) {
@@ -679,7 +680,7 @@ long long Program::allocate(std::vector<void*>& bases, std::vector<void*>& owned
     }
     owned.push_back(p);
     bases[i] = p;
-    if (zero && cudaMemset(p, 0, b) != cudaSuccess) throw std::runtime_error("zeroing workspace " + slots[i].name + " failed");
+    if (cudaMemset(p, zero ? 0 : 0xFF, b) != cudaSuccess) throw std::runtime_error("clearing workspace " + slots[i].name + " failed");
     if (!slots[i].init.empty() &&
         cudaMemcpy(p, slots[i].init.data(), slots[i].init.size() * sizeof(double),
                    cudaMemcpyHostToDevice) != cudaSuccess)

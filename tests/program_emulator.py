@@ -38,7 +38,8 @@ class Emulator:
             size = {0: 8, 1: 16, 2: 1}[s["dt"]] * s["numel"]
             groups.setdefault(b, []).append((i, s, size))
         for b, members in groups.items():
-            raw = bytearray(max(sz for _, _, sz in members))
+            # workspace starts as NaN (all-ones bytes): an op that reads what no op wrote shows up
+            raw = bytearray(b"\xff" * max(sz for _, _, sz in members))
             for i, s, _ in members:
                 dt = {0: np.float64, 1: np.complex128, 2: np.uint8}[s["dt"]]
                 arr = np.frombuffer(raw, dtype=dt, count=s["numel"])
