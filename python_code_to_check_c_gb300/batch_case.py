@@ -6,7 +6,7 @@ Each system (seeded DF integrals, x/y/z dipoles) gets 24 trajectories -- 3
 polarisations x A in {0.001, 0.002, 0.005, 0.01} x w0 in {0.5, 0.923}, E(t) =
 A sin(w0 t), dt = 0.005 -- advanced together by one batched system in the
 mixed-precision form (5 slices), from its ground state (device DIIS, FP64,
-8 vectors, max residual 1e-10).  Launch shapes come from the autotuner.  The
+8 vectors, max residual 1e-10; the MP2 guess where DIIS diverges).  Launch shapes come from the autotuner.  The
 four systems run concurrently (one host thread and one stream each).  Prints
 one JSON line: aggregate trajectory-steps/s over --steps graph replays, per
 system rates, and the worst dipole error of the three A = 0.01, w0 = 0.923
@@ -32,13 +32,29 @@ DT = 0.005
 
 
 def ground_state(sysm):
+    """Device DIIS; where it diverges (the seeded integrals grow with n: at
+    o=18, v=82 the MP2 correlation energy is about -46 Eh) the MP2 guess
+    (t1 = 0, lambda = t) is the start state instead, and the record says so."""
     eng = CCEngine.from_system(sysm)
-    t2 = mp2_guess(sysm.tei(), np.linalg.eigh(sysm.fock)[0], sysm.o)
-    t1 = np.zeros((sysm.o, sysm.v))
-    E, nt, t1, t2 = eng.ground_state("CCSD", 0, t1, t2, maxsize=8, maxiter=100, E_min=0.0, r_tol=1e-10)
-    El, nl, l1, l2 = eng.ground_state("CCSD", 1, t1, t2, t1, t2, maxsize=8, maxiter=100, E_min=0.0, r_tol=1e-10)
+    tei = sysm.tei()
+    t2g = mp2_guess(tei, np.linalg.eigh(sysm.fock)[0], sysm.o)
+    e_mp2 = 0.25 * float(np.sum(tei[: sysm.o, : sysm.o, sysm.o:, sysm.o:] * t2g))
+    t1g = np.zeros((sysm.o, sysm.v))
+    E, nt, t1, t2 = eng.ground_state("CCSD", 0, t1g, t2g, maxsize=8, maxiter=100, E_min=0.0, r_tol=1e-10)
+    ok = np.isfinite(E) and bool(torch.isfinite(torch.view_as_real(t2)).all())
+    info = {"E_mp2": e_mp2}
+    if ok:
+        El, nl, l1, l2 = eng.ground_state("CCSD", 1, t1, t2, t1, t2, maxsize=8, maxiter=100, E_min=0.0,
+                                          r_tol=1e-10)
+        ok = np.isfinite(El) and bool(torch.isfinite(torch.view_as_real(l2)).all())
+        info.update({"start": "DIIS ground state", "E_corr": E, "t_iter": nt, "l_iter": nl})
+    if not ok:
+        t1 = torch.zeros((sysm.o, sysm.v), dtype=torch.complex128, device="cuda")
+        t2 = torch.as_tensor(t2g.astype(np.complex128), device="cuda")
+        l1, l2 = t1.clone(), t2.clone()
+        info["start"] = "MP2 guess (DIIS diverges on this seeded system)"
     eng.close()
-    return (t1, t2, l1, l2), {"E_corr": E, "t_iter": nt, "l_iter": nl}
+    return (t1, t2, l1, l2), info
 
 
 def main():
