@@ -13,7 +13,8 @@ trajectory-steps per second.  The same line reports the plain FP64 GPU form
 (one trajectory, the reference's arithmetic), the mixed form on one
 trajectory, |d mu| of the z / A=0.002 / w0=0.923 trajectory against the FP64
 form, the end-to-end rate with host buffers, the roofline of the dominant
-kernel and the CPU oracle on the host cores.
+kernel, the cost of a pulse gradient by reverse mode relative to the forward
+(``adjoint``, FP64, --adjoint-steps steps) and the CPU oracle on the host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--precision fp64|mixed|auto] [--workload NAME] [--method CCSD|CC2] [--nb 24]
@@ -44,6 +45,9 @@ AMPS = (0.001, 0.002, 0.005, 0.01)
 W0S = (0.5, 0.923)
 POLS = (0, 1, 2)
 REF_TRAJ = (2, 0.002, 0.923)  # the single-trajectory configuration (z, A, w0)
+# DRAM bytes per launch of the step's dominant kernels, from one ncu capture of the same
+# contraction at 8 trajectories scaled by 3 (traffic grows with the trajectory count)
+TRAFFIC_PER_LAUNCH = {("ccsd_t2:mnij,mnab->ijab", 24): 3 * (51.46e6 + 0.55e6)}
 
 
 def parse():
@@ -58,6 +62,7 @@ def parse():
     p.add_argument("--nb", type=int, default=24, help="trajectories advanced together (24 = 3 pol x 4 A x 2 w0)")
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--adjoint-steps", type=int, default=100, help="pulse-gradient cost measurement (0: skip)")
     return p.parse_args()
 
 
@@ -182,6 +187,45 @@ def ground_state(sysm, method, dev):
     El, nl, l1, l2 = eng.ground_state(method, 1, t1, t2, t1, t2, maxsize=8, maxiter=100, E_min=0.0, r_tol=1e-10)
     eng.close()
     return (t1, t2, l1, l2), {"E_corr": E, "pseudo_E": El, "t_iterations": nt, "l_iterations": nl}
+
+
+def adjoint_cost(sysm, method, gs, nsteps):
+    """Gradient of J = sum_n dt cos(0.8 t_n) Re mu_z(t_n) with respect to a 32-bump
+    pulse (A = 0.003, w0 = 0.923, c_k ~ U(0.5, 1.5)), dt = 0.01, FP64, every step
+    kept: seconds of the reverse mode over seconds of the forward, and dJ/dA
+    against a central difference (h = 1e-5)."""
+    import torch
+
+    from python_code_to_check_c_gb300.engine import CCEngine
+    from python_code_to_check_c_gb300.pulse import Pulse, cosine_weights, pulse_gradient
+    eng = CCEngine.from_system(sysm)
+    dt = 0.01
+    rng = np.random.default_rng(4)
+    spacing = nsteps * dt / 31
+    pulse = Pulse(A=0.003, w0=0.923, c=rng.uniform(0.5, 1.5, 32), t_first=0.0, spacing=spacing, sigma=spacing)
+    w = cosine_weights(0.0, dt, nsteps)
+
+    def J_of(pu):
+        _, traj = eng.propagate(method, gs, 0.0, dt, nsteps, pu.field(), precs=-1)
+        return float(np.sum(w * traj.cpu().numpy().real))
+
+    J_of(pulse)
+    pulse_gradient(eng, method, gs, pulse, 0.0, dt, min(nsteps, 10), w[:min(nsteps, 10)], checkpoint=nsteps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = J_of(pulse)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Jg, gA, gw, gc = pulse_gradient(eng, method, gs, pulse, 0.0, dt, nsteps, w, checkpoint=nsteps)
+    t_grad = time.perf_counter() - t0
+    h = 1e-5
+    pp = Pulse(pulse.A + h, pulse.w0, pulse.c, pulse.t_first, pulse.spacing, pulse.sigma)
+    pm = Pulse(pulse.A - h, pulse.w0, pulse.c, pulse.t_first, pulse.spacing, pulse.sigma)
+    fd = (J_of(pp) - J_of(pm)) / (2 * h)
+    eng.close()
+    return {"steps": nsteps, "dt": dt, "bumps": 32, "precision": "fp64", "checkpoint": "every step kept",
+            "forward_s": t_fwd, "gradient_s": t_grad, "grad_over_fwd": t_grad / t_fwd, "J": J,
+            "dJ_dA": gA, "dJ_dA_central_difference": fd, "rel_err": abs(gA - fd) / max(abs(fd), 1e-300)}
 
 
 def timed(fn):
@@ -346,11 +390,17 @@ def run_ours(args, rank, world, local_rank):
         achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "hbm", "unit": "GB/s", "peak_source": "measured HBM copy (MEASURED_PEAKS.json)"}
+    traffic = TRAFFIC_PER_LAUNCH.get((tag, nb))
     roof.update({"kernel": tag, "achieved": achieved, "peak": peak, "frac": achieved / peak,
-                 "traffic": None, "launches_per_step": dom["n"], "share_of_step": dom["ms"] / tot,
+                 "traffic": traffic, "traffic_source": "ncu capture at 8 trajectories x 3" if traffic else None,
+                 "launches_per_step": dom["n"], "share_of_step": dom["ms"] / tot,
                  "avg_launch_ms": dom["ms"] / dom["n"]})
     top = sorted(by.items(), key=lambda kv: -kv[1]["ms"])[:6]
     breakdown = [{"kernel": k[0], "tc": k[1], "share": a["ms"] / tot, "launches": a["n"]} for k, a in top]
+
+    adj = None
+    if args.adjoint_steps > 0:
+        adj = adjoint_cost(sysm, args.method, gs, args.adjoint_steps)
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -374,7 +424,7 @@ def run_ours(args, rank, world, local_rank):
                          f"{sysm.n ** 4 * 8 / 2**20:.0f} MiB integrals (> 129 MB L2), no flush",
                    "ground_state": gs_info},
         "roofline": roof, "kernel_breakdown": breakdown, "cpu_baseline": cpu, "e2e": e2e,
-        "fp64_form": fp64, "single_trajectory_mixed": single_mixed,
+        "fp64_form": fp64, "single_trajectory_mixed": single_mixed, "adjoint": adj,
         "gpu_launches": launches, "launches_per_step": launches / args.steps, "clocks": clk.summary(),
         "finite": finite,
     }

@@ -79,6 +79,17 @@ struct ProgInst {
   }
 };
 
+// Buffer sharing costs concurrency (shared buffers order otherwise independent
+// ops), so it is used only where memory matters: programs whose workspace
+// slots add up to more than this.
+constexpr long long kShareMinBytes = 1LL << 30;
+long long workspace_estimate(const Program& p) {
+  long long b = 0;
+  for (size_t i = kNumFixedSlots; i < p.slots.size(); ++i)
+    if (!p.slots[i].fixed) b += p.slots[i].numel * elem_bytes(p.slots[i].dt);
+  return b;
+}
+
 // contractions with at least this many multiply-adds (and K >= 64) use the
 // tensor-core slice products in the mixed-precision mode
 constexpr long long kTcMinMacs = 1LL << 18;
@@ -195,7 +206,7 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
   p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
-  if (s->share_mem) p.plan_memory();
+  if (s->share_mem && workspace_estimate(p) > kShareMinBytes) p.plan_memory();
   pi->bases.assign(p.slots.size(), nullptr);
   pi->bytes = p.allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;
@@ -213,7 +224,7 @@ ProgInst& get_density(tdcc_system s) {
   pi->prog->batch(s->nb);
   pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   pi->prog->analyse({});
-  if (s->share_mem) pi->prog->plan_memory();
+  if (s->share_mem && workspace_estimate(*pi->prog) > kShareMinBytes) pi->prog->plan_memory();
   pi->bases.assign(pi->prog->slots.size(), nullptr);
   pi->bytes = pi->prog->allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;

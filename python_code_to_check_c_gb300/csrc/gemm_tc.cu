@@ -65,59 +65,6 @@ __device__ __forceinline__ void decomp_tc(const ModeGroup& g, int l, long long& 
 constexpr int kExpBias = 4096;
 __device__ __forceinline__ int row_exp(int biased) { return biased > 0 ? biased - kExpBias : 0; }
 
-// Pass 1: per packed row, the binary exponent e of max |x| (max = f 2^e,
-// f in [0.5, 1)).  One warp per (row, 256-wide K range), warp max, one
-// atomicMax per warp.
-__global__ void __launch_bounds__(256) pack_rowmax_kernel(const PackArgs p) {
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  const int kr = (p.K + 255) / 256;
-  if (warp >= (long long)p.rows * p.nb * kr) return;
-  const long long rg = warp / kr;  // logical row over all batches
-  const int z = (int)(rg / p.rows), m = (int)(rg % p.rows), k0 = (int)(warp % kr) * 256;
-  long long roff;
-  decomp_tc(p.gr, m, roff);
-  roff += z * p.bs;
-  int* exps = p.exps + (size_t)z * p.rows_pad;
-  // max |x| on the bit patterns (for finite doubles the order of |x| is the
-  // order of the unsigned bits with the sign cleared): integer ops only
-  const unsigned long long* src = static_cast<const unsigned long long*>(p.src);
-  constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
-  unsigned long long mre = 0, mim = 0;
-#pragma unroll 4
-  for (int j = 0; j < 8; ++j) {
-    const int k = k0 + lane + 32 * j;
-    if (k < p.K) {
-      long long ko;
-      decomp_tc(p.gk, k, ko);
-      const long long e = roff + ko;
-      if (p.cplx) {
-        mre = max(mre, src[2 * e] & kAbs);
-        mim = max(mim, src[2 * e + 1] & kAbs);
-      } else {
-        mre = max(mre, src[e] & kAbs);
-      }
-    }
-  }
-  for (int d = 16; d > 0; d >>= 1) {
-    mre = max(mre, __shfl_xor_sync(0xffffffffu, mre, d));
-    mim = max(mim, __shfl_xor_sync(0xffffffffu, mim, d));
-  }
-  if (lane == 0) {
-    // max = f 2^e with f in [0.5, 1): e = biased exponent - 1022.  The real
-    // and imaginary rows of a complex row share one exponent (that of the
-    // larger part), so that the slice-product epilogue combines
-    // re*re - im*im and re*im + im*re exactly in integers.
-    const unsigned long long mx = max(mre, mim);
-    const int E = (int)(mx >> 52);
-    if (mx != 0) {
-      const int eb = (E > 0 ? E - 1022 : -1022) + kExpBias;
-      atomicMax(&exps[p.cplx ? 2 * m : m], eb);
-      if (p.cplx) atomicMax(&exps[2 * m + 1], eb);
-    }
-  }
-}
-
 // floor(|x| 2^(nbits - e)) as an integer, from the bits of x (exact; no FP64
 // arithmetic).  Requires |x| < 2^e and nbits <= 56, so the result < 2^nbits.
 __device__ __forceinline__ unsigned long long fixed_point(double x, int e, int nbits) {
@@ -131,39 +78,77 @@ __device__ __forceinline__ unsigned long long fixed_point(double x, int e, int n
   return M >> (-sh);
 }
 
-// Pass 2: one block per packed row, threads over K: |x| 2^-e truncated to
-// 7S bits and cut into S signed 7-bit digits (|q_s| <= 127, exact in BF16):
-//   x 2^-e ~= sum_s q_s 2^(-7s).   Zero in the padding.
-__global__ void __launch_bounds__(256) pack_slice_kernel(const PackArgs p) {
-  const int prg = blockIdx.x;             // packed row over all batches
-  const int z = prg / p.rows_pad, pr = prg - z * p.rows_pad;
-  const int m = p.cplx ? (pr >> 1) : pr;
-  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
-  const double* src = static_cast<const double*>(p.src);
-  const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
-  const size_t rowbase = (size_t)prg * p.K_pad;
+// One block per logical row (per batch; the real and imaginary rows of a
+// complex row together): pass 1 takes the binary exponent e of the row's
+// max |x| (max = f 2^e, f in [0.5, 1); integer ops on the bit patterns, the
+// order of |x| for finite doubles), pass 2 cuts |x| 2^-e truncated to 7S
+// bits into S signed 7-bit digits (|q_s| <= 127, exact in BF16):
+//   x 2^-e ~= sum_s q_s 2^(-7s).
+// The real and imaginary rows share e, so that the slice-product epilogue
+// combines re*re - im*im and re*im + im*re exactly in integers.  Padding rows
+// and columns are written as zero (exponent entry 0).
+__global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
+  const int per = p.cplx ? 2 : 1;
+  const int rl_pad = p.rows_pad / per;  // logical rows per batch, padding included
+  const int z = blockIdx.x / rl_pad, m = blockIdx.x - z * rl_pad;
   const bool live = m < p.rows;
   long long ro = 0;
   if (live) {
     decomp_tc(p.gr, m, ro);
     ro += z * p.bs;
   }
-  const int e = row_exp(p.exps[prg]);
+  const unsigned long long* bits = static_cast<const unsigned long long*>(p.src);
+  const double* src = static_cast<const double*>(p.src);
+  constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
+  unsigned long long mx = 0;
+  if (live)
+    for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
+      long long ko;
+      decomp_tc(p.gk, k, ko);
+      const long long e = ro + ko;
+      if (p.cplx)
+        mx = max(mx, max(bits[2 * e] & kAbs, bits[2 * e + 1] & kAbs));
+      else
+        mx = max(mx, bits[e] & kAbs);
+    }
+  for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+  __shared__ unsigned long long wmax[8];
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = max(mx, wmax[w]);
+  const int E = (int)(mx >> 52);
+  const int eb = mx != 0 ? (E > 0 ? E - 1022 : -1022) + kExpBias : 0;
+  const size_t prow = (size_t)z * p.rows_pad + (size_t)m * per;  // first packed row
+  if (threadIdx.x == 0) {
+    p.exps[prow] = eb;
+    if (p.cplx) p.exps[prow + 1] = eb;
+  }
+  const int e = row_exp(eb);
   const int nbits = 7 * p.S;
-  for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < p.K_pad; k += gridDim.y * blockDim.x) {
-    unsigned long long f = 0ull;
-    bool neg = false;
+  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+  const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
+  for (int k = threadIdx.x; k < p.K_pad; k += blockDim.x) {
+    double x[2] = {0.0, 0.0};
     if (live && k < p.K) {
       long long ko;
       decomp_tc(p.gk, k, ko);
       const long long el = ro + ko;
-      const double x = p.cplx ? src[2 * el + (pr & 1)] : src[el];
-      f = fixed_point(x, e, nbits);
-      neg = x < 0.0;
+      if (p.cplx) {
+        x[0] = src[2 * el];
+        x[1] = src[2 * el + 1];
+      } else {
+        x[0] = src[el];
+      }
     }
-    for (int s = 0; s < p.S; ++s) {
-      const int q = (int)((f >> (7 * (p.S - 1 - s))) & 127ull);
-      out[s * plane + rowbase + k] = __float2bfloat16_rn((float)(neg ? -q : q));
+    for (int part = 0; part < per; ++part) {
+      const unsigned long long f = fixed_point(x[part], e, nbits);
+      const bool neg = x[part] < 0.0;
+      const size_t base = (prow + part) * p.K_pad + k;
+      for (int s = 0; s < p.S; ++s) {
+        const int q = (int)((f >> (7 * (p.S - 1 - s))) & 127ull);
+        out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -q : q));
+      }
     }
   }
 }
@@ -689,17 +674,11 @@ static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, i
 }
 
 cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
-  if (p.nb < 1) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMemsetAsync(p.exps, 0, (size_t)p.nb * p.rows_pad * sizeof(int), st);
-  if (e != cudaSuccess) return e;
-  const long long warps = (long long)p.rows * p.nb * ((p.K + 255) / 256);
-  if (warps > 0) {
-    pack_rowmax_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(p);
-    count_launch();
-  }
-  const int threads = p.K_pad >= 256 ? 256 : p.K_pad;
-  const int by = (p.K_pad + threads - 1) / threads > 8 ? 8 : (p.K_pad + threads - 1) / threads;
-  pack_slice_kernel<<<dim3((unsigned)((long long)p.nb * p.rows_pad), by), threads, 0, st>>>(p);
+  if (p.nb < 1 || p.rows_pad % (p.cplx ? 2 : 1) != 0) return cudaErrorInvalidValue;
+  const long long blocks = (long long)p.nb * (p.rows_pad / (p.cplx ? 2 : 1));
+  if (blocks > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;
+  const int threads = p.K_pad >= 256 ? 256 : ((p.K_pad + 31) / 32) * 32;
+  pack_kernel<<<(unsigned)blocks, threads, 0, st>>>(p);
   count_launch();
   return cudaGetLastError();
 }
