@@ -1067,6 +1067,7 @@ int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, con
           Op best_op = op;
           for (int tile = 0; tile < kNumTiles; ++tile)
             for (int split = 0; split < 2; ++split) {
+              if (!tile_fits(tile, op.g.M)) continue;
               Op c = op;
               Program::plan_gemm(c, split == 1 && op.zeroed, tile);
               if (c.tile == op.tile && c.g.nsplit == op.g.nsplit) continue;

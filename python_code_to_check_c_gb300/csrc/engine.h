@@ -350,9 +350,10 @@ void coalesce(AddArgs& a);
 void build_adjoint(const Program& f, Program& a, std::vector<int>& adj_of);
 
 // FP64 contraction tile shapes (kernels.cu)
-constexpr int kNumTiles = 5;
+constexpr int kNumTiles = 7;
 extern const int kTiles[kNumTiles][2];
 int choose_tile(long long M, long long N);
+bool tile_fits(int tile, long long M);  // the M tiles fit the launch grid
 
 // kernel launchers (kernels.cu)
 cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cudaStream_t st);

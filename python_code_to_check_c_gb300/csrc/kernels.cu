@@ -135,8 +135,11 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
       Bs[kk][br] = bv;
     }
     __syncthreads();
+    // the last K step of a short K range stops at its end (K = o = 10 would
+    // otherwise spend 6 of 16 multiply-adds on zero padding)
+    const int kmax = min(GBK, kend - k0);
 #pragma unroll 4
-    for (int kk = 0; kk < GBK; ++kk) {
+    for (int kk = 0; kk < kmax; ++kk) {
       TA a[TM];
       TB b[TN];
 #pragma unroll
@@ -203,12 +206,15 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
 }
 
 // tile shapes: {BM, BN}
-const int kTiles[kNumTiles][2] = {{64, 64}, {32, 64}, {64, 32}, {32, 32}, {16, 16}};
+const int kTiles[kNumTiles][2] = {{64, 64}, {32, 64}, {64, 32}, {32, 32}, {16, 16}, {16, 128}, {128, 16}};
+
+bool tile_fits(int t, long long M) { return (M + kTiles[t][0] - 1) / kTiles[t][0] <= 65535; }  // grid.y
 
 int choose_tile(long long M, long long N) {
   int best = 0;
   double bc = 1e300;
   for (int t = 0; t < kNumTiles; ++t) {
+    if (!tile_fits(t, M)) continue;
     const long long bm = kTiles[t][0], bn = kTiles[t][1];
     // padded multiply-adds, with a small penalty for less operand reuse
     const double pen = (bm * bn >= 4096) ? 1.0 : (bm * bn >= 1024) ? 1.06 : 1.15;
@@ -228,6 +234,8 @@ static void launch_typed(int tile, dim3 grid, const GemmArgs& g, cudaStream_t st
     case 1: gemm_f64_kernel<AC, BC, CC, 32, 64, 2, 4><<<grid, 256, 0, st>>>(g); break;
     case 2: gemm_f64_kernel<AC, BC, CC, 64, 32, 4, 2><<<grid, 256, 0, st>>>(g); break;
     case 3: gemm_f64_kernel<AC, BC, CC, 32, 32, 2, 2><<<grid, 256, 0, st>>>(g); break;
+    case 5: gemm_f64_kernel<AC, BC, CC, 16, 128, 1, 8><<<grid, 256, 0, st>>>(g); break;
+    case 6: gemm_f64_kernel<AC, BC, CC, 128, 16, 8, 1><<<grid, 256, 0, st>>>(g); break;
     default: gemm_f64_kernel<AC, BC, CC, 16, 16, 1, 1><<<grid, 256, 0, st>>>(g); break;
   }
 }

@@ -25,7 +25,7 @@ class Emulator:
     read every forward value after the forward ran -- the runtime turns the
     sharing off for them too)."""
 
-    def __init__(self, prog, o, v, n_mu=3, share=True):
+    def __init__(self, prog, o, v, n_mu=3, share=True, zero=False):
         self.p = prog
         self.o, self.v, self.n = o, v, o + v
         self.n_mu = n_mu
@@ -38,8 +38,10 @@ class Emulator:
             size = {0: 8, 1: 16, 2: 1}[s["dt"]] * s["numel"]
             groups.setdefault(b, []).append((i, s, size))
         for b, members in groups.items():
-            # workspace starts as NaN (all-ones bytes): an op that reads what no op wrote shows up
-            raw = bytearray(b"\xff" * max(sz for _, _, sz in members))
+            # workspace starts as NaN (all-ones bytes): an op that reads what no op wrote shows
+            # up; reverse-mode programs accumulate, their workspace starts at zero (zero=True),
+            # as the runtime allocates it
+            raw = bytearray((b"\x00" if zero else b"\xff") * max(sz for _, _, sz in members))
             for i, s, _ in members:
                 dt = {0: np.float64, 1: np.complex128, 2: np.uint8}[s["dt"]]
                 arr = np.frombuffer(raw, dtype=dt, count=s["numel"])

@@ -61,7 +61,7 @@ def _adjoint(sysm, tei, method, block, x, w, nb, ef=None):
     if ef is None:
         ef, _ = _forward(sysm, tei, method, block, x, nb)
     adj = adjoint_program_json(o, v, method, block, 3, nb)
-    ea = Emulator(adj, o, v)
+    ea = Emulator(adj, o, v, zero=True)
     for s, b in ef.bufs.items():
         if s < adj["nfwd"]:
             ea.bufs[s] = b
@@ -195,7 +195,7 @@ def test_adjoint_phase_split(small, method, block):
     ef.bind(S_RES, np.zeros(3, dtype=np.complex128))
     ef.run("setup")
     ef.run("prologue")
-    ea = Emulator(adj, o, v)
+    ea = Emulator(adj, o, v, zero=True)
     aof = adj["adj_of"]
     for s, a in enumerate(aof):
         if a >= 0 and adj["slots"][a]["fixed"]:
