@@ -145,6 +145,14 @@ int tdcc_ground_state(tdcc_system s, int method, int mode, void* t1, void* t2, v
    cores, which tests use at small sizes.                                  */
 int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k);
 
+/* Workspace buffer sharing (no counterpart in the reference): a program whose
+   workspace slots add up to more than min_bytes lets slots with disjoint
+   lifetimes within one phase share memory (fewer bytes, some ops ordered
+   that could otherwise run concurrently).  min_bytes < 0: the default
+   (1 GiB); 0: always.  Reverse mode (tdcc_adjoint) turns sharing off for the
+   system, as it reads every forward value after a stage ran.             */
+int tdcc_set_memory_sharing(tdcc_system s, long long min_bytes);
+
 /* Synchronises the device and reports TDCC_ERR_CUDA if a kernel of this
    system recorded an error (a tensor-core kernel whose bounded wait
    expired); clears the flag.                                              */

@@ -8,6 +8,7 @@
 
 #include "../../include/tdcc.h"
 #include "engine.h"
+#include "gemm_tc.h"
 #include "ground.h"
 #include "rk4.h"
 
@@ -113,6 +114,7 @@ struct tdcc_system_s {
   int nb = 1;                       // trajectories advanced together
   bool share_mem = true;            // workspace slots with disjoint lifetimes share memory (off once
                                     // reverse mode is used: it reads every forward value after a stage)
+  long long share_min = -1;         // sharing threshold in bytes (-1: kShareMinBytes)
   std::vector<tdcc_field> h_fields; // per-trajectory fields (tdcc_set_fields)
   std::vector<int> h_pol;
   std::unique_ptr<ProgInst> rhs[2][4];
@@ -206,7 +208,7 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
   p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
-  if (s->share_mem && workspace_estimate(p) > kShareMinBytes) p.plan_memory();
+  if (s->share_mem && workspace_estimate(p) > (s->share_min < 0 ? kShareMinBytes : s->share_min)) p.plan_memory();
   pi->bases.assign(p.slots.size(), nullptr);
   pi->bytes = p.allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;
@@ -224,7 +226,8 @@ ProgInst& get_density(tdcc_system s) {
   pi->prog->batch(s->nb);
   pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
   pi->prog->analyse({});
-  if (s->share_mem && workspace_estimate(*pi->prog) > kShareMinBytes) pi->prog->plan_memory();
+  if (s->share_mem && workspace_estimate(*pi->prog) > (s->share_min < 0 ? kShareMinBytes : s->share_min))
+    pi->prog->plan_memory();
   pi->bases.assign(pi->prog->slots.size(), nullptr);
   pi->bytes = pi->prog->allocate(pi->bases, pi->owned);
   s->ws_bytes += pi->bytes;
@@ -567,6 +570,14 @@ int tdcc_set_precision(tdcc_system s, int mode, int slices) {
   reset_programs(s);
   s->prec_mode = mode;
   s->slices = slices;
+  return TDCC_OK;
+}
+
+int tdcc_set_memory_sharing(tdcc_system s, long long min_bytes) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (min_bytes == s->share_min) return TDCC_OK;
+  reset_programs(s);
+  s->share_min = min_bytes;
   return TDCC_OK;
 }
 
@@ -1087,24 +1098,30 @@ int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, con
           const double t_cur = time_op(pi, op);
           double best = t_cur;
           TcArgs best_a = op.tc;
-          if (op.zeroed)
-            for (int sp : {1, 2, 3, 4, 6, 8, 12, 16}) {
-              if (sp > op.tc.kblocks) break;
+          for (int variant = 0; variant < 2; ++variant) {
+            if (variant == 1 && op.tc.S > TcNarrow::STAGES) continue;
+            for (int sp : {0, 1, 2, 3, 4, 6, 8, 12, 16}) {  // 0: the current split
               Op c = op;
-              c.tc.kb_per_split = (c.tc.kblocks + sp - 1) / sp;
-              c.tc.nsplit = (c.tc.kblocks + c.tc.kb_per_split - 1) / c.tc.kb_per_split;
-              c.tc.atomic = c.tc.nsplit > 1 ? 1 : 0;
-              if (c.tc.nsplit == op.tc.nsplit) continue;
-              if (!c.tc.atomic && !c.tc.acc) continue;  // plain store needs one writer per element
+              c.tc.variant = variant;
+              if (sp > 0) {
+                if (!op.zeroed || sp > op.tc.kblocks) continue;
+                c.tc.kb_per_split = (c.tc.kblocks + sp - 1) / sp;
+                c.tc.nsplit = (c.tc.kblocks + c.tc.kb_per_split - 1) / c.tc.kb_per_split;
+                c.tc.atomic = c.tc.nsplit > 1 ? 1 : 0;
+                if (c.tc.nsplit == op.tc.nsplit) continue;
+                if (!c.tc.atomic && !c.tc.acc) continue;  // plain store needs one writer per element
+              }
+              if (c.tc.variant == op.tc.variant && c.tc.nsplit == op.tc.nsplit) continue;
               const double t = time_op(pi, c);
               if (t < best * 0.97) {
                 best = t;
                 best_a = c.tc;
               }
             }
+          }
           before += t_cur;
           after += best;
-          if (best_a.nsplit != op.tc.nsplit) {
+          if (best_a.nsplit != op.tc.nsplit || best_a.variant != op.tc.variant) {
             op.tc = best_a;
             ++tuned;
           }

@@ -19,11 +19,14 @@
 // operands are combined with a lane-pair shuffle and written through the
 // same strided output decoder as the FP64 kernel.
 //
-// Pipeline: 2 + TC_EPI_WARPS warps.  Warp 0 issues TMA loads
-// (SWIZZLE_128B) into an 8-stage shared-memory ring, one (A_s, B_s) slice
-// pair per stage; warp 1 owns TMEM and issues the MMAs from one thread; the
-// other warps drain TMEM, TC_EPI_WARPS / 4 per TMEM lane quarter, each
-// taking a slice of the tile's columns.
+// Pipeline (two variants, TcCfg in gemm_tc.h): warp 0 issues TMA loads
+// (SWIZZLE_128B) into a shared-memory ring, one (A_s, B_s) slice pair per
+// stage; warp 1 owns TMEM and issues the MMAs from one thread; the other
+// warps drain TMEM, EPI / 4 per TMEM lane quarter, each taking a slice of
+// the tile's columns.  The wide variant (64 columns, 8 stages, 16 drain
+// warps) runs one CTA per SM; the narrow one (32 columns, 5 stages, 8 drain
+// warps) two, so that one CTA's drain overlaps the other's MMAs -- for
+// contractions with short K, whose time is per-CTA latency.
 // Every wait has an iteration limit: on expiry the kernel records an error
 // code, stops issuing work, waits (bounded) for its own operations and frees
 // TMEM before returning.
@@ -253,14 +256,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // ---------------------------------------------------------------------------
 constexpr int kWaitLimit = 1 << 22;
 
+template <class C>
 struct TcShared {
-  uint64_t full[TC_STAGES];
-  uint64_t empty[TC_STAGES];
+  uint64_t full[C::STAGES];
+  uint64_t empty[C::STAGES];
   uint64_t accfull, accempty, done;
   uint32_t tmem;
   volatile int abort;  // set by any role on an expired wait; polled by all
-  long long col_off[TC_BN];  // output offset of each logical column of the tile (-1: outside)
-  int col_exp[TC_BN];        // exponent of each packed column of B
+  long long col_off[C::BN];  // output offset of each logical column of the tile (-1: outside)
+  int col_exp[C::BN];        // exponent of each packed column of B
 };
 
 // x * 2^E rounded to nearest (ties to even) from the integer's bits: no FP64
@@ -290,30 +294,31 @@ __device__ __forceinline__ double scaled_i64_to_double(long long x, int E) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (mant & 0x000FFFFFFFFFFFFFull)));
 }
 
-__device__ __forceinline__ void fail(TcShared* sh, int* err, int code) {
+template <class SH>
+__device__ __forceinline__ void fail(SH* sh, int* err, int code) {
   sh->abort = 1;
   atomicCAS(err, 0, code);
 }
 
-template <bool AC, bool BC>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+template <bool AC, bool BC, class C>
+__global__ void __launch_bounds__(C::THREADS, C::MINB)
     ozaki_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs g) {
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  uint8_t* stA = sm;                                   // TC_STAGES x 16 KB
-  uint8_t* stB = sm + TC_STAGES * TC_A_BYTES;          // TC_STAGES x 8 KB
-  TcShared* sh = (TcShared*)(stB + TC_STAGES * TC_B_BYTES);
+  uint8_t* stA = sm;                                   // STAGES x 16 KB
+  uint8_t* stB = sm + C::STAGES * TC_A_BYTES;          // STAGES x BN x 128 B
+  TcShared<C>* sh = (TcShared<C>*)(stB + C::STAGES * C::B_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = g.S;
   const int ncols = g.tmem_cols;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < TC_STAGES; ++i) {
+    for (int i = 0; i < C::STAGES; ++i) {
       mbar_init(smem_u32(&sh->full[i]), 1);
       mbar_init(smem_u32(&sh->empty[i]), 1);
     }
     mbar_init(smem_u32(&sh->accfull), 1);
-    mbar_init(smem_u32(&sh->accempty), 32 * TC_EPI_WARPS);
+    mbar_init(smem_u32(&sh->accempty), 32 * C::EPI);
     mbar_init(smem_u32(&sh->done), 1);
     sh->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -344,26 +349,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int it = 0;
       for (int kb = kb0; kb < kb1 && !sh->abort; ++kb)
         for (int s = 0; s < S && !sh->abort; ++s, ++it) {
-          const int st = it % TC_STAGES;
-          const uint32_t ph = (uint32_t)((it / TC_STAGES) & 1);
+          const int st = it % C::STAGES;
+          const uint32_t ph = (uint32_t)((it / C::STAGES) & 1);
           if (!mbar_wait(smem_u32(&sh->empty[st]), ph ^ 1u, kWaitLimit)) {
             fail(sh, g.err, 1);
             break;
           }
           const uint32_t fb = smem_u32(&sh->full[st]);
-          mbar_expect_tx(fb, TC_A_BYTES + TC_B_BYTES);
+          mbar_expect_tx(fb, TC_A_BYTES + C::B_BYTES);
           tma3d(smem_u32(stA + st * TC_A_BYTES), &tmA, kb * TC_BK, rowA0 + mt * TC_BM, s, fb);
-          tma3d(smem_u32(stB + st * TC_B_BYTES), &tmB, kb * TC_BK, rowB0 + nt * TC_BN, s, fb);
+          tma3d(smem_u32(stB + st * C::B_BYTES), &tmB, kb * TC_BK, rowB0 + nt * C::BN, s, fb);
         }
       // drain: every issued load must land before the CTA exits
       const int issued = it;
-      for (int j = (issued > TC_STAGES ? issued - TC_STAGES : 0); j < issued; ++j)
-        mbar_wait(smem_u32(&sh->full[j % TC_STAGES]), (uint32_t)((j / TC_STAGES) & 1), kWaitLimit);
+      for (int j = (issued > C::STAGES ? issued - C::STAGES : 0); j < issued; ++j)
+        mbar_wait(smem_u32(&sh->full[j % C::STAGES]), (uint32_t)((j / C::STAGES) & 1), kWaitLimit);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      constexpr uint32_t id = idesc_bf16(TC_BM, TC_BN);
+      constexpr uint32_t id = idesc_bf16(TC_BM, C::BN);
       int it = 0;
       for (int c = 0; c < nchunks && !sh->abort; ++c) {
         if (c > 0 && !mbar_wait(smem_u32(&sh->accempty), (uint32_t)((c - 1) & 1), kWaitLimit)) {
@@ -377,7 +382,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           bool ok = true;
           for (int s = 0; s < S; ++s) {
             const int j = it + s;
-            if (!mbar_wait(smem_u32(&sh->full[j % TC_STAGES]), (uint32_t)((j / TC_STAGES) & 1), kWaitLimit)) {
+            if (!mbar_wait(smem_u32(&sh->full[j % C::STAGES]), (uint32_t)((j / C::STAGES) & 1), kWaitLimit)) {
               ok = false;
               break;
             }
@@ -388,14 +393,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
           for (int L = 2; L <= S + 1; ++L) {
-            const uint32_t dacc = tmem + (uint32_t)((L - 2) * TC_BN);
+            const uint32_t dacc = tmem + (uint32_t)((L - 2) * C::BN);
             int np = 0;
             for (int s = 1; s < L; ++s) {
               const int t = L - s;
               if (s > S || t > S) continue;
-              const int sa = (it + s - 1) % TC_STAGES, sb = (it + t - 1) % TC_STAGES;
+              const int sa = (it + s - 1) % C::STAGES, sb = (it + t - 1) % C::STAGES;
               const uint64_t da = sdesc(smem_u32(stA + sa * TC_A_BYTES));
-              const uint64_t db = sdesc(smem_u32(stB + sb * TC_B_BYTES));
+              const uint64_t db = sdesc(smem_u32(stB + sb * C::B_BYTES));
 #pragma unroll
               for (int k = 0; k < TC_BK / 16; ++k) {
                 const uint32_t accf = (first && np == 0 && k == 0) ? 0u : 1u;
@@ -405,7 +410,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
           }
           first = false;
-          for (int s = 0; s < S; ++s) umma_commit(smem_u32(&sh->empty[(it + s) % TC_STAGES]));
+          for (int s = 0; s < S; ++s) umma_commit(smem_u32(&sh->empty[(it + s) % C::STAGES]));
         }
         umma_commit(smem_u32(&sh->accfull));
       }
@@ -414,12 +419,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_wait(smem_u32(&sh->done), 0, kWaitLimit);
     }
   } else {
-    // ---------------- epilogue (warps 2 .. 2 + TC_EPI_WARPS - 1) ----------------
-    // TC_EPI_WARPS / 4 warps per TMEM lane quarter, each owning a slice of the
+    // ---------------- epilogue (warps 2 .. 2 + C::EPI - 1) ----------------
+    // C::EPI / 4 warps per TMEM lane quarter, each owning a slice of the
     // tile's columns: the drain is latency-bound per warp, so the work is
     // spread over warps.
-    constexpr int kWq = TC_EPI_WARPS / 4;   // warps per lane quarter
-    constexpr int kCw = TC_BN / kWq;        // packed columns per warp (multiple of 16)
+    constexpr int kWq = C::EPI / 4;   // warps per lane quarter
+    constexpr int kCw = C::BN / kWq;        // packed columns per warp (multiple of 16)
     const int q = warp & 3;             // TMEM lane quarter this warp may access
     const int hcol = (warp - 2) >> 2;   // column slice of this warp
     const int row = q * 32 + lane;      // tile row == TMEM lane
@@ -432,29 +437,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int u = 7 * ((S < 5 ? S : 5) + 1);
     {
       // per-tile column data, shared by all rows: output offsets and B exponents
-      const int t = threadIdx.x - 64;  // 0 .. 32 * TC_EPI_WARPS - 1
-      constexpr int ncl = BC ? TC_BN / 2 : TC_BN;
+      const int t = threadIdx.x - 64;  // 0 .. 32 * C::EPI - 1
+      constexpr int ncl = BC ? C::BN / 2 : C::BN;
       if (t < ncl) {
         const int n = nt * ncl + t;
         long long o = -1;
         if (n < g.N) decomp_tc(g.gnC, n, o);
         sh->col_off[t] = o;
       }
-      if (t < TC_BN) sh->col_exp[t] = row_exp(g.expB[rowB0 + nt * TC_BN + t]);
-      asm volatile("bar.sync 1, %0;" ::"n"(32 * TC_EPI_WARPS) : "memory");  // the epilogue warps
+      if (t < C::BN) sh->col_exp[t] = row_exp(g.expB[rowB0 + nt * C::BN + t]);
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * C::EPI) : "memory");  // the epilogue warps
     }
     // Row data and the staging tile of this warp (final chunk): the operand
     // ring is idle once the last accumulators are complete.
     const int prow = mt * TC_BM + row;          // packed row of A (within the batch)
     const int m = AC ? (prow >> 1) : prow;
     const bool odd = AC && (lane & 1);
-    constexpr int ncol_log = BC ? TC_BN / 2 : TC_BN;  // logical output columns in this tile
+    constexpr int ncol_log = BC ? C::BN / 2 : C::BN;  // logical output columns in this tile
     constexpr int rows_out = AC ? 16 : 32;             // logical output rows of this warp
     constexpr int RS = ncol_log + 1;                    // staging row stride (double2), padded
     double2* stage = reinterpret_cast<double2*>(sm) + (size_t)q * (32 * RS);
     const int lr = AC ? (lane >> 1) : lane;            // this lane's staging row
     const uint32_t tl = (uint32_t)(q * 32) << 16;      // TMEM lane base of this warp
-    const uint32_t t64 = (uint32_t)(S * TC_BN);        // int64 partial sums: 2 words per column
+    const uint32_t t64 = (uint32_t)(S * C::BN);        // int64 partial sums: 2 words per column
     bool ok = true;
     for (int c = 0; c < nchunks; ++c) {
       // warp-uniform decisions: tcgen05.ld/st and the shuffles below are collective
@@ -499,7 +504,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           uint32_t lv[3][16];
 #pragma unroll
           for (int i = 0; i < 3; ++i)
-            if (L0 + i <= S + 1) tmem_ld16_nowait(tmem + tl + (uint32_t)((L0 + i - 2) * TC_BN + j0), lv[i]);
+            if (L0 + i <= S + 1) tmem_ld16_nowait(tmem + tl + (uint32_t)((L0 + i - 2) * C::BN + j0), lv[i]);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
@@ -683,37 +688,58 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st) {
+template <class C>
+static cudaError_t launch_variant(const TcArgs& a0, const void* packA, const void* packB, cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(ozaki_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         TC_SMEM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(ozaki_kernel<true, true, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(ozaki_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               TC_SMEM_BYTES);
+      e = cudaFuncSetAttribute(ozaki_kernel<true, false, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(ozaki_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               TC_SMEM_BYTES);
+      e = cudaFuncSetAttribute(ozaki_kernel<false, true, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(ozaki_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               TC_SMEM_BYTES);
+      e = cudaFuncSetAttribute(ozaki_kernel<false, false, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+    // all of L1 as shared memory, so that MINB CTAs fit on an SM
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ozaki_kernel<true, true, C>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ozaki_kernel<true, false, C>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ozaki_kernel<false, true, C>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(ozaki_kernel<false, false, C>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  if (a.nb < 1 || a.nsplit < 1 || (long long)a.nsplit * a.kb_per_split < a.kblocks) return cudaErrorInvalidValue;
+  TcArgs a = a0;
+  if (a.S > C::STAGES) return cudaErrorInvalidValue;  // the ring holds one K block's slices
+  int cols = 32;
+  while (cols < (a.S + 2) * C::BN) cols *= 2;  // level accumulators + int64 partial sums
+  if (cols > 512 / C::MINB) return cudaErrorInvalidValue;
+  a.tmem_cols = cols;
+  if (a.rowsB_pad % C::BN != 0) return cudaErrorInvalidValue;
   const CUtensorMap ma = slice_map(packA, a.S, (a.bat_a ? a.nb : 1) * a.rowsA_pad, a.kblocks * TC_BK, TC_BM);
-  const CUtensorMap mb = slice_map(packB, a.S, (a.bat_b ? a.nb : 1) * a.rowsB_pad, a.kblocks * TC_BK, TC_BN);
-  dim3 grid(a.rowsB_pad / TC_BN, a.rowsA_pad / TC_BM, (unsigned)((long long)a.nb * a.nsplit));
+  const CUtensorMap mb = slice_map(packB, a.S, (a.bat_b ? a.nb : 1) * a.rowsB_pad, a.kblocks * TC_BK, C::BN);
+  dim3 grid(a.rowsB_pad / C::BN, a.rowsA_pad / TC_BM, (unsigned)((long long)a.nb * a.nsplit));
   if (a.ac && a.bc)
-    ozaki_kernel<true, true><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<true, true, C><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
   else if (a.ac)
-    ozaki_kernel<true, false><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<true, false, C><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
   else if (a.bc)
-    ozaki_kernel<false, true><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<false, true, C><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
   else
-    ozaki_kernel<false, false><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(ma, mb, a);
+    ozaki_kernel<false, false, C><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
   count_launch();
   return cudaGetLastError();
+}
+
+cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st) {
+  if (a.nb < 1 || a.nsplit < 1 || (long long)a.nsplit * a.kb_per_split < a.kblocks) return cudaErrorInvalidValue;
+  return a.variant == 1 ? launch_variant<TcNarrow>(a, packA, packB, st) : launch_variant<TcWide>(a, packA, packB, st);
 }
 
 }  // namespace tdcc

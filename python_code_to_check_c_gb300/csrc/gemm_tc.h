@@ -9,15 +9,25 @@
 namespace tdcc {
 
 constexpr int TC_BM = 128;                   // UMMA M (rows of A per CTA)
-constexpr int TC_BN = 64;                    // UMMA N (rows of B per CTA)
+constexpr int TC_BN = 64;                    // packed B rows are padded to this (both variants)
 constexpr int TC_BK = 64;                    // K per TMA box (128 B of BF16)
-constexpr int TC_STAGES = 8;                 // shared-memory ring depth
 constexpr int TC_CHUNK_KB = 16;              // 1024-wide K chunks (exact FP32 sums)
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
-constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
-constexpr int TC_SMEM_BYTES = 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 2048;
 constexpr int TC_MAX_SLICES = 6;
-constexpr int TC_EPI_WARPS = 16;             // TMEM drain warps (four per lane quarter)
-constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;  // + TMA producer warp + MMA warp
+
+// Kernel variants: tile width BN (UMMA N), ring depth, TMEM-drain warps and
+// CTAs per SM.  The ring must hold the S slices of one K block (STAGES >= S).
+template <int BN_, int STAGES_, int EPI_, int MINB_>
+struct TcCfg {
+  static constexpr int BN = BN_, STAGES = STAGES_, EPI = EPI_, MINB = MINB_;
+  static constexpr int B_BYTES = BN * TC_BK * 2;
+  static constexpr int THREADS = 64 + 32 * EPI;  // + TMA producer warp + MMA warp
+  static constexpr int SMEM = 1024 + STAGES * (TC_A_BYTES + B_BYTES) + 2048;
+};
+// one CTA per SM: 64-wide tile, 8 stages, 16 drain warps (four per lane quarter)
+using TcWide = TcCfg<64, 8, 16, 1>;
+// two CTAs per SM (one's drain overlaps the other's MMAs): 32-wide tile, 5
+// stages, 8 drain warps; TMEM (S + 2) x 32 <= 256 columns, so S <= 5
+using TcNarrow = TcCfg<32, 5, 8, 2>;
 
 }  // namespace tdcc

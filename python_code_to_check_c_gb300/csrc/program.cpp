@@ -1072,6 +1072,8 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     a.nsplit = (int)splits;
     a.atomic = splits > 1 ? 1 : 0;
     t.zeroed = a.acc || a.atomic;  // split K is allowed (a zero op precedes when not accumulating)
+    // short K: the narrow variant (two CTAs per SM overlap their latencies)
+    a.variant = (a.kb_per_split == 1 && S <= 5) ? 1 : 0;
     t.bytes = (long long)S * (nbA * rA + nbB * rB) * Kp * 2 + nbt * M * N * elem_bytes(op.dtc);
     t.reads = {pa.pk_dst, pb.pk_dst};
     if (a.acc || a.atomic) t.reads.push_back(op.sc);

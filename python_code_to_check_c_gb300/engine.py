@@ -121,6 +121,11 @@ class CCEngine:
         """Which contractions the mixed mode sends to the tensor cores."""
         check(self.lib.tdcc_set_tc_policy(self.handle, int(min_macs), int(min_k)), "tdcc_set_tc_policy")
 
+    def set_memory_sharing(self, min_bytes: int = -1):
+        """Workspace buffer sharing above min_bytes per program (-1: default
+        1 GiB, 0: always)."""
+        check(self.lib.tdcc_set_memory_sharing(self.handle, int(min_bytes)), "tdcc_set_memory_sharing")
+
     def autotune(self, method: str, state, reps: int = 3):
         """Picks the launch shape of every contraction by timing candidates
         on this system (``tdcc_autotune``); returns (ops changed, summed
