@@ -192,7 +192,8 @@ def ground_state(sysm, method, dev):
 def adjoint_cost(sysm, method, gs, nsteps):
     """Gradient of J = sum_n dt cos(0.8 t_n) Re mu_z(t_n) with respect to a 32-bump
     pulse (A = 0.003, w0 = 0.923, c_k ~ U(0.5, 1.5)), dt = 0.01, FP64, every step
-    kept: seconds of the reverse mode over seconds of the forward, and dJ/dA
+    kept (with the forward intermediates the reverse-mode programs read):
+    seconds of the reverse mode over seconds of the forward, and dJ/dA
     against a central difference (h = 1e-5)."""
     import torch
 
@@ -224,6 +225,7 @@ def adjoint_cost(sysm, method, gs, nsteps):
     fd = (J_of(pp) - J_of(pm)) / (2 * h)
     eng.close()
     return {"steps": nsteps, "dt": dt, "bumps": 32, "precision": "fp64", "checkpoint": "every step kept",
+            "reverse_reads": "forward intermediates recorded by the forward step graph (activation records)",
             "forward_s": t_fwd, "gradient_s": t_grad, "grad_over_fwd": t_grad / t_fwd, "J": J,
             "dJ_dA": gA, "dJ_dA_central_difference": fd, "rel_err": abs(gA - fd) / max(abs(fd), 1e-300)}
 

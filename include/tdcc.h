@@ -153,6 +153,14 @@ int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k);
    system, as it reads every forward value after a stage ran.             */
 int tdcc_set_memory_sharing(tdcc_system s, long long min_bytes);
 
+/* Reverse mode's forward intermediates (no counterpart in the reference):
+   mode 1 keeps, per step of a checkpoint segment, the intermediates each
+   block's reverse-mode program reads (written by the captured forward step);
+   mode 0 runs each stage's forward ops again before its reverse; mode -1
+   (default) keeps them when the records need at most half the free device
+   memory.  Both give the same gradients up to summation order.          */
+int tdcc_set_adjoint_store(tdcc_system s, int mode);
+
 /* Synchronises the device and reports TDCC_ERR_CUDA if a kernel of this
    system recorded an error (a tensor-core kernel whose bounded wait
    expired); clears the flag.                                              */

@@ -35,6 +35,14 @@ struct ProgInst {
   std::unique_ptr<Program> prog;
   std::vector<void*> bases;
   size_t nfwd = 0;           // reverse-mode programs: slots [0, nfwd) are the forward program's
+  // reverse-mode programs of the RHS blocks: the forward slots they read that
+  // forward ops write once per step (prologue) or once per stage, with their
+  // offsets (8-byte words) in one step's activation record
+  std::vector<int> act_slot;
+  std::vector<char> act_stage;
+  std::vector<long long> act_off8;
+  long long act_pro8 = 0, act_stage8 = 0;
+  long long act_step8() const { return act_pro8 + 4 * act_stage8; }
   std::vector<void*> owned;  // this program's workspace allocations
   long long bytes = 0;
   bool setup_done = false;   // integral-only ops (e.g. packed integral blocks) ran
@@ -115,6 +123,8 @@ struct tdcc_system_s {
   bool share_mem = true;            // workspace slots with disjoint lifetimes share memory (off once
                                     // reverse mode is used: it reads every forward value after a stage)
   long long share_min = -1;         // sharing threshold in bytes (-1: kShareMinBytes)
+  int adj_store = -1;               // reverse mode keeps forward intermediates (1), recomputes them
+                                    // (0), or keeps them when they fit (-1)
   std::vector<tdcc_field> h_fields; // per-trajectory fields (tdcc_set_fields)
   std::vector<int> h_pol;
   std::unique_ptr<ProgInst> rhs[2][4];
@@ -238,6 +248,7 @@ ProgInst& get_density(tdcc_system s) {
 }
 
 void build_program(Program& p, int method, int block, int n_mu, int nb);
+void plan_activations(ProgInst& ai, const Program& fwd);
 void reset_programs(tdcc_system s);
 
 // Reverse-mode program of (method, block); block 4 = density.  Its slots
@@ -265,8 +276,63 @@ ProgInst& get_adj(tdcc_system s, int method, int block) {
   s->ws_bytes += pi->bytes;
   pi->setup_done = true;  // no integral-only ops in a reverse-mode program
   pi->dag.init(pi->prog->ops.size(), 4);
+  if (block < 4) plan_activations(*pi, *get_rhs(s, method, block).prog);
   slot = std::move(pi);
   return *slot;
+}
+
+// The activation record of one RK4 step for reverse mode: the forward slots
+// that the reverse-mode program reads and that forward ops write outside the
+// integral-only setup.  A slot written by a stage op holds one value per
+// stage; the others one per step.  Binding the reverse-mode program to the
+// record gives it the values the forward step computed, so it need not run
+// the forward ops again.
+void plan_activations(ProgInst& ai, const Program& fwd) {
+  std::vector<char> rd(ai.nfwd, 0), pro(ai.nfwd, 0), stg(ai.nfwd, 0);
+  for (const Op& op : ai.prog->ops)
+    for (int r : op.reads)
+      if (r >= 0 && r < (int)ai.nfwd) rd[r] = 1;
+  for (const Op& op : fwd.ops) {
+    if (op.write < 0 || op.write >= (int)ai.nfwd) continue;
+    if (Program::in_phase(op, Program::STAGE))
+      stg[op.write] = 1;
+    else if (Program::in_phase(op, Program::PROLOGUE))
+      pro[op.write] = 1;
+  }
+  ai.act_slot.clear();
+  ai.act_stage.clear();
+  ai.act_off8.clear();
+  ai.act_pro8 = ai.act_stage8 = 0;
+  for (int pass = 0; pass < 2; ++pass)
+    for (size_t i = 0; i < ai.nfwd; ++i) {
+      if (!rd[i] || !(pro[i] || stg[i]) || (pass == 1) != (stg[i] != 0)) continue;
+      const SlotInfo& si = fwd.slots[i];
+      const long long w = (si.numel * elem_bytes(si.dt) + 7) / 8;
+      long long& acc = pass ? ai.act_stage8 : ai.act_pro8;
+      ai.act_slot.push_back((int)i);
+      ai.act_stage.push_back((char)pass);
+      ai.act_off8.push_back(acc);
+      acc += (w + 31) / 32 * 32;  // 256-byte aligned entries
+    }
+}
+
+// copies of one phase's activations (stage 0: prologue) into the step store
+void store_activations(const StepCtx* ctx, const ProgInst& ai, const ProgInst& pi, const StepStore& ss, int b,
+                       int stage, cudaStream_t st) {
+  ActTable t{};
+  const long long base = stage == 0 ? 0 : ai.act_pro8 + (stage - 1) * ai.act_stage8;
+  for (size_t j = 0; j < ai.act_slot.size(); ++j) {
+    if ((ai.act_stage[j] != 0) != (stage != 0)) continue;
+    const int sl = ai.act_slot[j];
+    const SlotInfo& si = pi.prog->slots[sl];
+    t.c[t.n++] = {static_cast<const double*>(pi.bases[sl]), base + ai.act_off8[j],
+                  (si.numel * elem_bytes(si.dt) + 7) / 8};
+    if (t.n == kMaxActCopies) {
+      CK(launch_act_store(ctx, t, ss.act[b], ss.act_stride[b], st));
+      t.n = 0;
+    }
+  }
+  CK(launch_act_store(ctx, t, ss.act[b], ss.act_stride[b], st));
 }
 
 void ensure_rk(tdcc_system s) {
@@ -347,12 +413,15 @@ void run_block(tdcc_system s, int method, int b, double2* const in[4], double2* 
   CK(pi.setup(st));
   CK(pi.exec(st, Program::PROLOGUE, pf ? &tm : nullptr));
   if (pf) pf->add_prog(tm, b, 0);
+  const ProgInst* act = ss && ss->act[b] ? s->adjp[method][b].get() : nullptr;
+  if (act) store_activations(s->ctx, *act, pi, *ss, b, 0, st);
   for (int stage = 1; stage <= 4; ++stage) {
     B[S_T1 + b] = stage == 1 ? in[b] : s->yin[b];
     B[S_F] = s->Fs + (stage == 1 ? 0 : stage < 4 ? 1 : 2) * nn;
     tm.clear();
     CK(pi.exec(st, Program::STAGE, pf ? &tm : nullptr));
     if (pf) pf->add_prog(tm, b, stage);
+    if (act) store_activations(s->ctx, *act, pi, *ss, b, stage, st);
     const double h = stage < 3 ? dt / 2.0 : dt;
     timed_launch(pf, st, "rk4_stage_axpy", b, stage, (double)n * 16 * (stage == 1 ? 3 : stage == 4 ? 3 : 5),
                  [&] { return launch_rk4_stage(in[b], s->kbuf[b], s->acc[b], s->yin[b], n, stage, h, st); });
@@ -578,6 +647,13 @@ int tdcc_set_memory_sharing(tdcc_system s, long long min_bytes) {
   if (min_bytes == s->share_min) return TDCC_OK;
   reset_programs(s);
   s->share_min = min_bytes;
+  return TDCC_OK;
+}
+
+int tdcc_set_adjoint_store(tdcc_system s, int mode) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (mode < -1 || mode > 1) return fail(TDCC_ERR_ARG, "mode must be -1, 0 or 1");
+  s->adj_store = mode;
   return TDCC_OK;
 }
 
@@ -1220,6 +1296,21 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
     double2* gE = alloc((size_t)nsteps * 4 * nb * 16);
     double2* traj = alloc((size_t)nsteps * nb * 16);
     double2* straj = alloc((size_t)K * nb * 16);
+    // activation records (forward intermediates per step) when they fit;
+    // otherwise each stage's forward ops run again before its reverse
+    bool use_act = false;
+    if (s->adj_store != 0) {
+      long long act8 = 0;
+      for (int b = 0; b < 4; ++b) act8 += get_adj(s, method, b).act_step8();
+      size_t fr = 0, tot = 0;
+      CK(cudaMemGetInfo(&fr, &tot));
+      use_act = s->adj_store == 1 || (double)K * act8 * 8 <= 0.5 * (double)fr;
+      for (int b = 0; b < 4 && use_act; ++b) {
+        const long long w = get_adj(s, method, b).act_step8();
+        ss.act_stride[b] = w;
+        ss.act[b] = w ? reinterpret_cast<double*>(alloc((size_t)K * w * 8)) : nullptr;
+      }
+    }
     CK(cudaMemsetAsync(gE, 0, (size_t)nsteps * 4 * nb * 16, m));
     const void* in[4] = {t1, t2, l1, l2};
     for (int b = 0; b < 4; ++b) CK(cudaMemcpyAsync(y[b], in[b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
@@ -1289,15 +1380,19 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
           for (int q = 0; q < 4; ++q) B[S_T1 + q] = yk(k, q);
           B[S_OUT] = s->kbuf[b];
           B[S_F] = Fk;
-          CK(pi.exec(m, Program::PROLOGUE));
+          if (!use_act) CK(pi.exec(m, Program::PROLOGUE));
           // a_k(s) = c w_s a_out, c = -i dt/6 (T) or +i dt/6 (Lambda)
           const double ci = (b == TDCC_T1 || b == TDCC_T2) ? -c6 : c6;
           for (int st = 0; st < 4; ++st) CK(launch_caxpy(ak[st], ay[b], nel(b), 0.0, wst[st] * ci, 0, m));
           for (int st = 4; st >= 1; --st) {
             B[S_T1 + b] = st == 1 ? yk(k, b) : ss.st[b][st - 2] + (size_t)k * ss.sst[b];
             B[S_F] = Fk + (size_t)(st == 1 ? 0 : st < 4 ? 1 : 2) * nb * nn;
-            CK(pi.exec(m, Program::STAGE));
+            if (!use_act) CK(pi.exec(m, Program::STAGE));
             for (size_t i = 0; i < ai.nfwd; ++i) ai.bases[i] = B[i];
+            if (use_act)
+              for (size_t j = 0; j < ai.act_slot.size(); ++j)
+                ai.bases[ai.act_slot[j]] = ss.act[b] + (size_t)k * ss.act_stride[b] + ai.act_off8[j] +
+                                           (ai.act_stage[j] ? ai.act_pro8 + (st - 1) * ai.act_stage8 : 0);
             CK(cudaMemcpyAsync(akin, ak[st - 1], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
             ai.bases[aof[S_OUT]] = akin;
             CK(cudaMemsetAsync(aY, 0, nel(b) * 16, m));

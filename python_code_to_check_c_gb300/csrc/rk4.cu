@@ -202,6 +202,24 @@ __global__ void step_store_kernel(const StepCtx* ctx, const double2* __restrict_
 
 static unsigned grid_for(long long n);
 
+__global__ void act_store_kernel(const StepCtx* ctx, ActTable t, double* base, long long stride8) {
+  const ActCopy c = t.c[blockIdx.y];
+  double* d = base + ctx->step * stride8 + c.off8;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < c.n8; i += (long long)gridDim.x * blockDim.x)
+    d[i] = c.src[i];
+}
+
+cudaError_t launch_act_store(const StepCtx* ctx, const ActTable& t, double* base, long long stride8,
+                             cudaStream_t st) {
+  if (t.n <= 0) return cudaSuccess;
+  long long mx = 0;
+  for (int j = 0; j < t.n; ++j) mx = t.c[j].n8 > mx ? t.c[j].n8 : mx;
+  dim3 grid(grid_for(mx), (unsigned)t.n);
+  act_store_kernel<<<grid, 256, 0, st>>>(ctx, t, base, stride8);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_step_store(const StepCtx* ctx, const double2* src, double2* dst_base, long long stride, long long n,
                               cudaStream_t st) {
   step_store_kernel<<<grid_for(n), 256, 0, st>>>(ctx, src, dst_base, stride, n);

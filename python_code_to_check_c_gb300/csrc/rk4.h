@@ -28,6 +28,9 @@ constexpr int kMaxTrajectories = 1024;
 // step k's state goes to y[b] + k * sy[b], the inputs of its stages 2..4 to
 // st[b][q] + k * sst[b], its dressed Fock matrices to fs + k * sfs (k is the
 // device step counter).
+// act[b] (when set) receives the forward intermediates that block b's
+// reverse-mode program reads: per step act_stride[b] 8-byte words, the
+// prologue values first, then the stage values of stages 1..4.
 struct StepStore {
   double2* y[4];
   long long sy[4];
@@ -35,7 +38,24 @@ struct StepStore {
   long long sst[4];
   double2* fs;
   long long sfs;
+  double* act[4];
+  long long act_stride[4];
 };
+
+// One launch copies up to kMaxActCopies buffers: entry j sends n8 8-byte
+// words from src to base + ctx->step * stride8 + off8.
+constexpr int kMaxActCopies = 32;
+struct ActCopy {
+  const double* src;
+  long long off8;
+  long long n8;
+};
+struct ActTable {
+  int n;
+  ActCopy c[kMaxActCopies];
+};
+cudaError_t launch_act_store(const StepCtx* ctx, const ActTable& t, double* base, long long stride8,
+                             cudaStream_t st);
 
 // dst_base + ctx->step * stride  <-  src  (n elements)
 cudaError_t launch_step_store(const StepCtx* ctx, const double2* src, double2* dst_base, long long stride, long long n,

@@ -126,6 +126,11 @@ class CCEngine:
         1 GiB, 0: always)."""
         check(self.lib.tdcc_set_memory_sharing(self.handle, int(min_bytes)), "tdcc_set_memory_sharing")
 
+    def set_adjoint_store(self, mode: int = -1):
+        """Reverse mode keeps the forward intermediates (1), recomputes them
+        (0), or keeps them when they fit in half the free memory (-1)."""
+        check(self.lib.tdcc_set_adjoint_store(self.handle, int(mode)), "tdcc_set_adjoint_store")
+
     def autotune(self, method: str, state, reps: int = 3):
         """Picks the launch shape of every contraction by timing candidates
         on this system (``tdcc_autotune``); returns (ops changed, summed
