@@ -1,7 +1,7 @@
 """Gradient of a dipole-response objective with respect to pulse parameters, on
 the GPU:  python -m python_code_to_check_c_gb300.adjoint_case
     [--workload ccsd_o10_v38] [--method CCSD] [--steps 500] [--dt 0.01] [--bumps 32]
-    [--checkpoint 50] [--precision fp64|mixed] [--fd 3]
+    [--checkpoint 50] [--precision fp64|mixed] [--fd 3] [--store -1|0|1]
 
 Pulse E(t) = A sin(w0 t) sum_k c_k phi_k(t), 32 Gaussian bumps spread over the
 propagation (sigma = spacing), c_k ~ U(0.5, 1.5) (seed 4), A = 0.003,
@@ -9,7 +9,10 @@ w0 = 0.923; objective J = sum_n dt cos(0.8 t_n) Re mu_z(t_n); start: the
 ground state (device DIIS, 8 vectors, max residual 1e-10).  Prints one JSON
 line: J, the forward time (captured step graphs), the reverse-mode time (its
 own forward with checkpoints + the backward), their ratio, and central
-differences (h = 1e-5) for the first --fd parameters (A, w0, c_0, ...)."""
+differences (h = 1e-5) for the first --fd parameters (A, w0, c_0, ...).
+--store: the reverse pass reads the forward intermediates recorded per step
+(1), runs each stage's forward ops again (0), or records them when they fit
+in half the free device memory (-1, default)."""
 from __future__ import annotations
 
 import argparse
@@ -34,6 +37,7 @@ def main():
     p.add_argument("--checkpoint", type=int, default=50)
     p.add_argument("--precision", default="fp64")
     p.add_argument("--fd", type=int, default=3)
+    p.add_argument("--store", type=int, default=-1)
     a = p.parse_args()
     sysm = synthetic_system(**WORKLOADS[a.workload])
     eng = CCEngine.from_system(sysm)
@@ -44,6 +48,7 @@ def main():
     st = (t1, t2, l1, l2)
     if a.precision == "mixed":
         eng.set_precision("mixed", 5)
+    eng.set_adjoint_store(a.store)
     T = a.steps * a.dt
     spacing = T / max(a.bumps - 1, 1)
     rng = np.random.default_rng(4)
@@ -87,7 +92,7 @@ def main():
                    "rel_err": abs(grads[k] - d) / max(abs(d), 1e-300)})
     print(json.dumps({
         "workload": a.workload, "method": a.method, "steps": a.steps, "dt": a.dt, "bumps": a.bumps,
-        "checkpoint": a.checkpoint, "precision": a.precision, "J": J, "J_from_adjoint_run": Jg,
+        "checkpoint": a.checkpoint, "precision": a.precision, "store": a.store, "J": J, "J_from_adjoint_run": Jg,
         "forward_s": t_fwd, "gradient_s": t_grad, "grad_over_fwd": t_grad / t_fwd,
         "gradient_norm": float(np.linalg.norm(grads)), "fd_checks": fd}))
     eng.close()

@@ -1271,7 +1271,7 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
     // ---- working memory for the call ----
     // segment store: per step the state, the inputs of stages 2..4 and the
     // dressed Fock matrices, written by the captured step graphs
-    std::vector<double2*> ck(4 * nseg), y(4), ay(4), ay2(4), ak(4);
+    std::vector<double2*> ck(4 * nseg), y(4), ay(4);
     if (nseg > 1)
       for (int j = 0; j < nseg; ++j)
         for (int b = 0; b < 4; ++b) ck[4 * j + b] = alloc(nel(b) * 16);
@@ -1279,21 +1279,27 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
     StepStore ss{};
     for (int b = 0; b < 4; ++b) {
       ss.sy[b] = ss.sst[b] = (long long)nel(b);
-      ss.y[b] = alloc((size_t)K * nel(b) * 16);
+      ss.y[b] = alloc((size_t)(K + 1) * nel(b) * 16);  // + the state after the segment
       for (int q = 0; q < 3; ++q) ss.st[b][q] = alloc((size_t)K * nel(b) * 16);
     }
     ss.sfs = 3LL * nb * nn;
     ss.fs = alloc((size_t)K * ss.sfs * 16);
+    // the four blocks' reverse passes run concurrently, each with its own
+    // scratch, its contributions to every block's cotangent (summed at the
+    // join in block order) and its slice of dJ/dE
+    double2 *ak[4][4], *akin[4], *aY[4], *aF[4], *contrib[4][4];
     for (int b = 0; b < 4; ++b) {
       ay[b] = alloc(nel(b) * 16);
-      ay2[b] = alloc(nel(b) * 16);
-      ak[b] = alloc(maxel * 16);
+      for (int st = 0; st < 4; ++st) ak[b][st] = alloc(maxel * 16);
+      akin[b] = alloc(maxel * 16);
+      aY[b] = alloc(maxel * 16);
+      aF[b] = alloc((size_t)nb * nn * 16);
+      for (int q = 0; q < 4; ++q)
+        contrib[b][q] = (q == b || s->adj_of[method][b][S_T1 + q] >= 0) ? alloc(nel(q) * 16) : nullptr;
     }
-    double2* akin = alloc(maxel * 16);
-    double2* aY = alloc(maxel * 16);
-    double2* aF = alloc((size_t)nb * nn * 16);
     double2* ares = alloc((size_t)nb * n_mu * 16);
-    double2* gE = alloc((size_t)nsteps * 4 * nb * 16);
+    const size_t gEn = (size_t)nsteps * 4 * nb;  // one block's dJ/dE
+    double2* gE = alloc(4 * gEn * 16);
     double2* traj = alloc((size_t)nsteps * nb * 16);
     double2* straj = alloc((size_t)K * nb * 16);
     // activation records (forward intermediates per step) when they fit;
@@ -1311,7 +1317,7 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
         ss.act[b] = w ? reinterpret_cast<double*>(alloc((size_t)K * w * 8)) : nullptr;
       }
     }
-    CK(cudaMemsetAsync(gE, 0, (size_t)nsteps * 4 * nb * 16, m));
+    CK(cudaMemsetAsync(gE, 0, 4 * gEn * 16, m));
     const void* in[4] = {t1, t2, l1, l2};
     for (int b = 0; b < 4; ++b) CK(cudaMemcpyAsync(y[b], in[b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
     CK(cudaStreamSynchronize(m));
@@ -1333,11 +1339,140 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
       }
     }
 
-    // ---- backward, segment by segment ----
+    // ---- backward: one captured graph per reverse step (with and without
+    //      the objective's dipole term), replayed for every step; it gathers
+    //      step k's stored values into fixed buffers, so one graph serves all
+    //      steps (k and the global step come from a device counter) ----
     for (int b = 0; b < 4; ++b) CK(cudaMemsetAsync(ay[b], 0, nel(b) * 16, m));
     const double c6 = dt / 6.0;
     const double wst[4] = {1.0, 2.0, 2.0, 1.0};
     const double hst[4] = {0.0, dt / 2.0, dt / 2.0, dt};  // Y(s) = y + h_s k_(s-1)
+    double2 *gy[4], *gyn[4], *gst[4][3];
+    double* gact[4] = {nullptr, nullptr, nullptr, nullptr};
+    GatherTable gt{};
+    auto gather = [&](const void* src, long long stride8, long long koff, void* dst, long long n8) {
+      if (gt.n == kMaxGather) throw std::runtime_error("reverse step gathers too many buffers");
+      gt.c[gt.n++] = {static_cast<const double*>(src), stride8, koff, static_cast<double*>(dst), n8};
+    };
+    for (int b = 0; b < 4; ++b) {
+      const long long w8 = (long long)nel(b) * 2;
+      gy[b] = alloc(nel(b) * 16);
+      gyn[b] = alloc(nel(b) * 16);
+      gather(ss.y[b], ss.sy[b] * 2, 0, gy[b], w8);
+      gather(ss.y[b], ss.sy[b] * 2, 1, gyn[b], w8);
+      for (int q = 0; q < 3; ++q) {
+        gst[b][q] = alloc(nel(b) * 16);
+        gather(ss.st[b][q], ss.sst[b] * 2, 0, gst[b][q], w8);
+      }
+      if (use_act && ss.act[b]) {
+        gact[b] = reinterpret_cast<double*>(alloc((size_t)ss.act_stride[b] * 8));
+        gather(ss.act[b], ss.act_stride[b], 0, gact[b], ss.act_stride[b]);
+      }
+    }
+    double2* gF = alloc((size_t)ss.sfs * 16);
+    gather(ss.fs, ss.sfs * 2, 0, gF, ss.sfs * 2);
+    RevCtx* rctx = reinterpret_cast<RevCtx*>(alloc(sizeof(RevCtx)));
+    double* wdev = reinterpret_cast<double*>(alloc((size_t)nsteps * 8));
+    CK(cudaMemcpyAsync(wdev, w_host, (size_t)nsteps * 8, cudaMemcpyHostToDevice, m));
+    const RevCtx rc_h{nsteps - 1, K};
+    CK(cudaMemcpyAsync(rctx, &rc_h, sizeof(RevCtx), cudaMemcpyHostToDevice, m));
+    CK(cudaStreamSynchronize(m));
+
+    auto reverse_step = [&](bool dipole) {
+      CK(launch_rev_gather(rctx, gt, m));
+      if (dipole) {  // the objective's dipole term at y_(n+1)
+        ProgInst& d = get_density(s);
+        ProgInst& ad = get_adj(s, method, 4);
+        const auto& aof = s->adj_of[method][4];
+        for (int q = 0; q < 4; ++q) d.bases[S_T1 + q] = gyn[q];
+        d.bases[S_RES] = s->res;
+        CK(d.exec(m, Program::ALL));
+        for (size_t i = 0; i < ad.nfwd; ++i) ad.bases[i] = d.bases[i];
+        CK(launch_dipole_cotangent(ares, s->d_pol, nb, n_mu, wdev, rctx, m));
+        ad.bases[aof[S_RES]] = ares;
+        for (int q = 0; q < 4; ++q)
+          if (aof[S_T1 + q] >= 0) ad.bases[aof[S_T1 + q]] = ay[q];
+        CK(ad.exec(m, Program::ALL));
+      }
+      // step adjoint: ay (of y_(n+1)) -> ay (of y_n); rounding taken as the
+      // identity.  Block b's update reads y_n only, so the four block
+      // reverse passes are independent.
+      CK(cudaEventRecord(s->ev_fork, m));
+      for (int b = 0; b < 4; ++b) {
+        cudaStream_t sb = s->bs[b];
+        CK(cudaStreamWaitEvent(sb, s->ev_fork, 0));
+        ProgInst& pi = get_rhs(s, method, b);
+        ProgInst& ai = get_adj(s, method, b);
+        const auto& aof = s->adj_of[method][b];
+        for (int q = 0; q < 4; ++q)
+          if (contrib[b][q]) CK(cudaMemsetAsync(contrib[b][q], 0, nel(q) * 16, sb));
+        auto& B = pi.bases;
+        for (int q = 0; q < 4; ++q) B[S_T1 + q] = gy[q];
+        B[S_OUT] = s->kbuf[b];
+        B[S_F] = gF;
+        if (!use_act) CK(pi.exec(sb, Program::PROLOGUE));
+        // a_k(s) = c w_s a_out, c = -i dt/6 (T) or +i dt/6 (Lambda)
+        const double ci = (b == TDCC_T1 || b == TDCC_T2) ? -c6 : c6;
+        for (int st = 0; st < 4; ++st) CK(launch_caxpy(ak[b][st], ay[b], nel(b), 0.0, wst[st] * ci, 0, sb));
+        for (int st = 4; st >= 1; --st) {
+          B[S_T1 + b] = st == 1 ? gy[b] : gst[b][st - 2];
+          B[S_F] = gF + (size_t)(st == 1 ? 0 : st < 4 ? 1 : 2) * nb * nn;
+          if (!use_act) CK(pi.exec(sb, Program::STAGE));
+          for (size_t i = 0; i < ai.nfwd; ++i) ai.bases[i] = B[i];
+          if (use_act)
+            for (size_t j = 0; j < ai.act_slot.size(); ++j)
+              ai.bases[ai.act_slot[j]] =
+                  gact[b] + ai.act_off8[j] + (ai.act_stage[j] ? ai.act_pro8 + (st - 1) * ai.act_stage8 : 0);
+          CK(cudaMemcpyAsync(akin[b], ak[b][st - 1], nel(b) * 16, cudaMemcpyDeviceToDevice, sb));
+          ai.bases[aof[S_OUT]] = akin[b];
+          CK(cudaMemsetAsync(aY[b], 0, nel(b) * 16, sb));
+          if (aof[S_T1 + b] >= 0) ai.bases[aof[S_T1 + b]] = aY[b];
+          if (aof[S_F] >= 0) {
+            CK(cudaMemsetAsync(aF[b], 0, (size_t)nb * nn * 16, sb));
+            ai.bases[aof[S_F]] = aF[b];
+          }
+          for (int q = 0; q < 4; ++q)
+            if (q != b && aof[S_T1 + q] >= 0) ai.bases[aof[S_T1 + q]] = contrib[b][q];
+          CK(ai.exec(sb, Program::STAGE));
+          if (aof[S_F] >= 0) CK(launch_field_grad(aF[b], s->mu, s->d_pol, n, nb, gE + b * gEn, rctx, st - 1, sb));
+          CK(launch_caxpy(contrib[b][b], aY[b], nel(b), 1.0, 0.0, 1, sb));
+          if (st > 1) CK(launch_caxpy(ak[b][st - 2], aY[b], nel(b), hst[st - 1], 0.0, 1, sb));
+        }
+        CK(ai.exec(sb, Program::PROLOGUE));
+        CK(cudaEventRecord(s->ev_join[b], sb));
+      }
+      for (int b = 0; b < 4; ++b) CK(cudaStreamWaitEvent(m, s->ev_join[b], 0));
+      for (int q = 0; q < 4; ++q)
+        CK(launch_sum4(ay[q], contrib[0][q], contrib[1][q], contrib[2][q], contrib[3][q], nel(q), m));
+      CK(launch_rev_advance(rctx, m));
+    };
+    struct Graphs {
+      cudaGraphExec_t g[2] = {nullptr, nullptr};
+      ~Graphs() {
+        for (auto x : g)
+          if (x) cudaGraphExecDestroy(x);
+      }
+    } rg;
+    bool need[2] = {false, false};
+    for (int i = 0; i < nsteps; ++i) need[w_host[i] != 0.0] = true;
+    long long per_step[2] = {0, 0};  // kernels per replay
+    for (int dip = 0; dip < 2; ++dip) {
+      if (!need[dip]) continue;
+      const long long before_capture = launch_count();
+      cudaGraph_t graph;
+      CK(cudaStreamBeginCapture(m, cudaStreamCaptureModeThreadLocal));
+      try {
+        reverse_step(dip != 0);
+      } catch (...) {
+        cudaStreamEndCapture(m, &graph);
+        throw;
+      }
+      CK(cudaStreamEndCapture(m, &graph));
+      CK(cudaGraphInstantiate(&rg.g[dip], graph, 0));
+      cudaGraphDestroy(graph);
+      per_step[dip] = launch_count() - before_capture;
+      count_launch(-per_step[dip]);  // captured, not executed
+    }
     for (int j = nseg - 1; j >= 0; --j) {
       const int k0 = j * K, kn = std::min(K, nsteps - k0);
       if (nseg > 1) {
@@ -1351,74 +1486,30 @@ int tdcc_adjoint(tdcc_system s, int method, const void* t1, const void* t2, cons
                                       nullptr, &ss);
         if (rs != TDCC_OK) return rs;
       }
-      auto yk = [&](int k, int b) { return k < kn ? ss.y[b] + (size_t)k * ss.sy[b] : y[b]; };
+      // the state after the segment follows its last stored step
+      for (int b = 0; b < 4; ++b)
+        CK(cudaMemcpyAsync(ss.y[b] + (size_t)kn * ss.sy[b], y[b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
       for (int k = kn - 1; k >= 0; --k) {
-        const int nstep = k0 + k;
-        // the objective's dipole term at y_(n+1)
-        if (w_host[nstep] != 0.0) {
-          ProgInst& d = get_density(s);
-          ProgInst& ad = get_adj(s, method, 4);
-          const auto& aof = s->adj_of[method][4];
-          for (int q = 0; q < 4; ++q) d.bases[S_T1 + q] = yk(k + 1, q);
-          d.bases[S_RES] = s->res;
-          CK(d.exec(m, Program::ALL));
-          for (size_t i = 0; i < ad.nfwd; ++i) ad.bases[i] = d.bases[i];
-          CK(launch_dipole_cotangent(ares, s->d_pol, nb, n_mu, w_host[nstep], m));
-          ad.bases[aof[S_RES]] = ares;
-          for (int q = 0; q < 4; ++q)
-            if (aof[S_T1 + q] >= 0) ad.bases[aof[S_T1 + q]] = ay[q];
-          CK(ad.exec(m, Program::ALL));
-        }
-        // step adjoint: ay (of y_(n+1)) -> ay2 (of y_n); rounding taken as the identity
-        for (int q = 0; q < 4; ++q) CK(cudaMemcpyAsync(ay2[q], ay[q], nel(q) * 16, cudaMemcpyDeviceToDevice, m));
-        double2* Fk = ss.fs + (size_t)k * ss.sfs;
-        for (int b = 0; b < 4; ++b) {
-          ProgInst& pi = get_rhs(s, method, b);
-          ProgInst& ai = get_adj(s, method, b);
-          const auto& aof = s->adj_of[method][b];
-          auto& B = pi.bases;
-          for (int q = 0; q < 4; ++q) B[S_T1 + q] = yk(k, q);
-          B[S_OUT] = s->kbuf[b];
-          B[S_F] = Fk;
-          if (!use_act) CK(pi.exec(m, Program::PROLOGUE));
-          // a_k(s) = c w_s a_out, c = -i dt/6 (T) or +i dt/6 (Lambda)
-          const double ci = (b == TDCC_T1 || b == TDCC_T2) ? -c6 : c6;
-          for (int st = 0; st < 4; ++st) CK(launch_caxpy(ak[st], ay[b], nel(b), 0.0, wst[st] * ci, 0, m));
-          for (int st = 4; st >= 1; --st) {
-            B[S_T1 + b] = st == 1 ? yk(k, b) : ss.st[b][st - 2] + (size_t)k * ss.sst[b];
-            B[S_F] = Fk + (size_t)(st == 1 ? 0 : st < 4 ? 1 : 2) * nb * nn;
-            if (!use_act) CK(pi.exec(m, Program::STAGE));
-            for (size_t i = 0; i < ai.nfwd; ++i) ai.bases[i] = B[i];
-            if (use_act)
-              for (size_t j = 0; j < ai.act_slot.size(); ++j)
-                ai.bases[ai.act_slot[j]] = ss.act[b] + (size_t)k * ss.act_stride[b] + ai.act_off8[j] +
-                                           (ai.act_stage[j] ? ai.act_pro8 + (st - 1) * ai.act_stage8 : 0);
-            CK(cudaMemcpyAsync(akin, ak[st - 1], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
-            ai.bases[aof[S_OUT]] = akin;
-            CK(cudaMemsetAsync(aY, 0, nel(b) * 16, m));
-            if (aof[S_T1 + b] >= 0) ai.bases[aof[S_T1 + b]] = aY;
-            if (aof[S_F] >= 0) {
-              CK(cudaMemsetAsync(aF, 0, (size_t)nb * nn * 16, m));
-              ai.bases[aof[S_F]] = aF;
-            }
-            for (int q = 0; q < 4; ++q)
-              if (q != b && aof[S_T1 + q] >= 0) ai.bases[aof[S_T1 + q]] = ay2[q];
-            CK(ai.exec(m, Program::STAGE));
-            if (aof[S_F] >= 0)
-              CK(launch_field_grad(aF, s->mu, s->d_pol, n, nb, gE + ((size_t)nstep * 4 + (st - 1)) * nb, m));
-            CK(launch_caxpy(ay2[b], aY, nel(b), 1.0, 0.0, 1, m));
-            if (st > 1) CK(launch_caxpy(ak[st - 2], aY, nel(b), hst[st - 1], 0.0, 1, m));
-          }
-          CK(ai.exec(m, Program::PROLOGUE));
-        }
-        std::swap(ay, ay2);
+        const int dip = w_host[k0 + k] != 0.0;
+        CK(cudaGraphLaunch(rg.g[dip], m));
+        count_launch(per_step[dip]);
       }
     }
     void* aout[4] = {a_t1, a_t2, a_l1, a_l2};
     for (int b = 0; b < 4; ++b)
       if (aout[b]) CK(cudaMemcpyAsync(aout[b], ay[b], nel(b) * 16, cudaMemcpyDeviceToDevice, m));
-    CK(cudaMemcpyAsync(gE_host, gE, (size_t)nsteps * 4 * nb * 16, cudaMemcpyDeviceToHost, m));
+    std::vector<double2> hg(4 * gEn);
+    CK(cudaMemcpyAsync(hg.data(), gE, 4 * gEn * 16, cudaMemcpyDeviceToHost, m));
     CK(cudaStreamSynchronize(m));
+    for (size_t i = 0; i < gEn; ++i) {
+      double re = 0.0, im = 0.0;
+      for (int b = 0; b < 4; ++b) {
+        re += hg[b * gEn + i].x;
+        im += hg[b * gEn + i].y;
+      }
+      gE_host[2 * i] = re;
+      gE_host[2 * i + 1] = im;
+    }
     CK(cudaEventRecord(s->ev_user, m));
     CK(cudaStreamWaitEvent(user, s->ev_user, 0));
   } catch (const std::exception& ex) {

@@ -155,8 +155,10 @@ __global__ void caxpy_kernel(double2* __restrict__ y, const double2* __restrict_
 // g[b] += sum_e aF[b][e] * (-mu[pol[b]][e]): dJ/dE of one RK4 stage, per
 // trajectory (F = fock - E mu_pol).  One block per trajectory, fixed-order sum.
 __global__ void __launch_bounds__(256) field_grad_kernel(const double2* __restrict__ aF, const double* __restrict__ mu,
-                                                         const int* __restrict__ pol, int nn, double2* __restrict__ g) {
+                                                         const int* __restrict__ pol, int nn, double2* __restrict__ g,
+                                                         const RevCtx* rc, int stage) {
   const int b = blockIdx.x;
+  if (rc) g += (rc->cur * 4 + stage) * (long long)gridDim.x;
   const double2* a = aF + (long long)b * nn;
   const double* m = mu + (long long)pol[b] * nn;
   double sr = 0.0, si = 0.0;
@@ -188,8 +190,9 @@ __global__ void __launch_bounds__(256) field_grad_kernel(const double2* __restri
 
 // a_res[b][k] = (k == pol[b]) ? w : 0  (cotangent of the recorded dipole component)
 __global__ void dipole_cotangent_kernel(double2* __restrict__ ares, const int* __restrict__ pol, int nb, int n_mu,
-                                        double w) {
+                                        const double* __restrict__ wts, const RevCtx* rc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double w = wts[rc->cur];
   if (i < nb * n_mu) ares[i] = make_double2((i % n_mu) == pol[i / n_mu] ? w : 0.0, 0.0);
 }
 
@@ -201,6 +204,30 @@ __global__ void step_store_kernel(const StepCtx* ctx, const double2* __restrict_
 }
 
 static unsigned grid_for(long long n);
+
+__global__ void rev_gather_kernel(const RevCtx* rc, GatherTable t) {
+  const GatherCopy c = t.c[blockIdx.y];
+  const double* src = c.src + (rc->cur % rc->K + c.koff) * c.stride8;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < c.n8; i += (long long)gridDim.x * blockDim.x)
+    c.dst[i] = src[i];
+}
+
+__global__ void rev_advance_kernel(RevCtx* rc) { rc->cur -= 1; }
+
+cudaError_t launch_rev_gather(const RevCtx* rc, const GatherTable& t, cudaStream_t st) {
+  if (t.n <= 0) return cudaSuccess;
+  long long mx = 0;
+  for (int j = 0; j < t.n; ++j) mx = t.c[j].n8 > mx ? t.c[j].n8 : mx;
+  rev_gather_kernel<<<dim3(grid_for(mx), (unsigned)t.n), 256, 0, st>>>(rc, t);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rev_advance(RevCtx* rc, cudaStream_t st) {
+  rev_advance_kernel<<<1, 1, 0, st>>>(rc);
+  count_launch();
+  return cudaGetLastError();
+}
 
 __global__ void act_store_kernel(const StepCtx* ctx, ActTable t, double* base, long long stride8) {
   const ActCopy c = t.c[blockIdx.y];
@@ -227,6 +254,26 @@ cudaError_t launch_step_store(const StepCtx* ctx, const double2* src, double2* d
   return cudaGetLastError();
 }
 
+__global__ void sum4_kernel(double2* __restrict__ y, const double2* x0, const double2* x1, const double2* x2,
+                            const double2* x3, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = y[i];
+    for (const double2* x : {x0, x1, x2, x3})
+      if (x) {
+        v.x += x[i].x;
+        v.y += x[i].y;
+      }
+    y[i] = v;
+  }
+}
+
+cudaError_t launch_sum4(double2* y, const double2* x0, const double2* x1, const double2* x2, const double2* x3,
+                        long long n, cudaStream_t st) {
+  sum4_kernel<<<grid_for(n), 256, 0, st>>>(y, x0, x1, x2, x3, n);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_caxpy(double2* y, const double2* x, long long n, double cr, double ci, int acc, cudaStream_t st) {
   caxpy_kernel<<<grid_for(n), 256, 0, st>>>(y, x, n, cr, ci, acc);
   count_launch();
@@ -234,14 +281,15 @@ cudaError_t launch_caxpy(double2* y, const double2* x, long long n, double cr, d
 }
 
 cudaError_t launch_field_grad(const double2* aF, const double* mu, const int* pol, int n, int nb, double2* g,
-                              cudaStream_t st) {
-  field_grad_kernel<<<nb, 256, 0, st>>>(aF, mu, pol, n * n, g);
+                              const RevCtx* rc, int stage, cudaStream_t st) {
+  field_grad_kernel<<<nb, 256, 0, st>>>(aF, mu, pol, n * n, g, rc, stage);
   count_launch();
   return cudaGetLastError();
 }
 
-cudaError_t launch_dipole_cotangent(double2* ares, const int* pol, int nb, int n_mu, double w, cudaStream_t st) {
-  dipole_cotangent_kernel<<<(nb * n_mu + 127) / 128, 128, 0, st>>>(ares, pol, nb, n_mu, w);
+cudaError_t launch_dipole_cotangent(double2* ares, const int* pol, int nb, int n_mu, const double* w,
+                                    const RevCtx* rc, cudaStream_t st) {
+  dipole_cotangent_kernel<<<(nb * n_mu + 127) / 128, 128, 0, st>>>(ares, pol, nb, n_mu, w, rc);
   count_launch();
   return cudaGetLastError();
 }

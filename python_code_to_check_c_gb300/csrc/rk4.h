@@ -69,12 +69,41 @@ cudaError_t launch_rk4_stage(const double2* y0, const double2* k, double2* acc, 
                              long long n, int s, double h, cudaStream_t st);
 cudaError_t launch_rk4_finish(const double2* y0, const double2* acc, double2* ynew, long long n,
                               double dt6, int sign, double scale, int do_round, cudaStream_t st);
-// reverse-mode helpers: y (+)= c x; g[b] += sum aF[b] * (-mu[pol[b]]); the
-// dipole cotangent a_res[b][k] = w * (k == pol[b])
+// Reverse-mode step counter: one captured reverse step serves every step of
+// a run.  It reads the global step cur (index cur % K within its checkpoint
+// segment of K steps) and ends by decrementing cur.
+struct RevCtx {
+  long long cur;
+  long long K;
+};
+// One launch gathers up to kMaxGather buffers: entry j sends n8 8-byte words
+// from src + (cur % K + koff) * stride8 to dst.
+constexpr int kMaxGather = 32;
+struct GatherCopy {
+  const double* src;
+  long long stride8;
+  long long koff;
+  double* dst;
+  long long n8;
+};
+struct GatherTable {
+  int n;
+  GatherCopy c[kMaxGather];
+};
+cudaError_t launch_rev_gather(const RevCtx* rc, const GatherTable& t, cudaStream_t st);
+cudaError_t launch_rev_advance(RevCtx* rc, cudaStream_t st);
+
+// reverse-mode helpers: y (+)= c x; g[b] += sum aF[b] * (-mu[pol[b]]) with
+// g = g_base + (cur * 4 + stage) * nb (g_base itself when rc is null); the
+// dipole cotangent a_res[b][k] = w[cur] * (k == pol[b])
 cudaError_t launch_caxpy(double2* y, const double2* x, long long n, double cr, double ci, int acc, cudaStream_t st);
-cudaError_t launch_field_grad(const double2* aF, const double* mu, const int* pol, int n, int nb, double2* g,
-                              cudaStream_t st);
-cudaError_t launch_dipole_cotangent(double2* ares, const int* pol, int nb, int n_mu, double w, cudaStream_t st);
+// y += x0 + x1 + x2 + x3 in that order (null terms skipped)
+cudaError_t launch_sum4(double2* y, const double2* x0, const double2* x1, const double2* x2, const double2* x3,
+                        long long n, cudaStream_t st);
+cudaError_t launch_field_grad(const double2* aF, const double* mu, const int* pol, int n, int nb, double2* g_base,
+                              const RevCtx* rc, int stage, cudaStream_t st);
+cudaError_t launch_dipole_cotangent(double2* ares, const int* pol, int nb, int n_mu, const double* w,
+                                    const RevCtx* rc, cudaStream_t st);
 // traj[step][b] = res[b][pol[b]]; step += 1
 cudaError_t launch_record_mu(StepCtx* ctx, const double2* res, int nb, double2* traj, double* times,
                              cudaStream_t st);
