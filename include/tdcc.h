@@ -261,6 +261,23 @@ int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, con
 long long tdcc_adjoint_program_json(int o, int v, int method, int block, int n_mu, int nb,
                                     char* buf, size_t len);
 
+/* Antisymmetrised two-electron integrals from density-fitting factors, on
+   the device (the integral provider; the reference reads psi4's
+   mo_spin_eri, CCSD_Helper.py:57-93):
+     tei[p,q,r,s] = sum_Q B[Q,p,r] B[Q,q,s] - sum_Q B[Q,p,s] B[Q,q,r]
+   B: device float64 [nq][n][n]; tei: device float64 [n][n][n][n] (written).
+   FP64 GEMM over Q, then an in-place antisymmetrisation.                   */
+int tdcc_tei_from_df(const double* B, int n, int nq, double* tei, void* stream);
+
+/* Dipole spectrum (Plots.py:20-25): the discrete Fourier transforms of
+   Re mu(t) and Im mu(t), each fftshift-ed:
+     Yr[j] = sum_n Re mu[n] exp(-2 pi i k n / N),  k = (j + N - N/2) mod N
+   (Yi likewise with Im mu), N = nsteps, mu[n * stride] device complex128;
+   Yr, Yi: device complex128 [N].  energy_ev (host [N], may be NULL): the
+   reference's axis (j - N/2) / (N dt) * 2 pi * 27.211 eV.                 */
+int tdcc_spectrum(const void* mu, long long nsteps, long long stride, double dt, void* Yr, void* Yi,
+                  double* energy_ev, void* stream);
+
 /* Dipole expectation value like tdcc_dipole, but without allocating any
    device memory and without a tdcc_system.  No counterpart in the reference
    (its dipole_moment, CCSD_Helper.py:1066, allocates numpy temporaries).

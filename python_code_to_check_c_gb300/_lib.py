@@ -69,6 +69,8 @@ SIGNATURES = {
     "tdcc_set_tc_policy": (_i, [_vp, _ll, _i]),
     "tdcc_set_memory_sharing": (_i, [_vp, _ll]),
     "tdcc_set_adjoint_store": (_i, [_vp, _i]),
+    "tdcc_tei_from_df": (_i, [_vp, _i, _i, _vp, _vp]),
+    "tdcc_spectrum": (_i, [_vp, _ll, _ll, _d, _vp, _vp, _vp, _vp]),
     "tdcc_ground_state": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_d), _i, _i, _d, _d,
                                ctypes.POINTER(_d), ctypes.POINTER(_i), _vp]),
     "tdcc_rhs": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

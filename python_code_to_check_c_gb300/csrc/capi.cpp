@@ -10,6 +10,7 @@
 #include "engine.h"
 #include "gemm_tc.h"
 #include "ground.h"
+#include "post.h"
 #include "rk4.h"
 
 #include <algorithm>
@@ -1562,6 +1563,73 @@ int tdcc_profile_step(tdcc_system s, int method, const void* t1, const void* t2,
     cudaEventDestroy(r.b);
   }
   *n_recs = k;
+  return TDCC_OK;
+}
+
+int tdcc_tei_from_df(const double* B, int n, int nq, double* tei, void* stream) {
+  if (!B || !tei) return fail(TDCC_ERR_ARG, "NULL argument");
+  if (n < 1 || nq < 1 || (long long)n * n > 0x7fffffffLL) return fail(TDCC_ERR_ARG, "bad sizes");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  try {
+    // X[p,q,r,s] = sum_Q B[Q,p,r] B[Q,q,s]: M modes (p, r), N modes (q, s), K = Q
+    const long long n2 = (long long)n * n, n3 = n2 * n;
+    Op op;
+    op.kind = OP_GEMM;
+    op.tag = "tei_from_df";
+    op.dta = op.dtb = op.dtc = R64;
+    GemmArgs& g = op.g;
+    g.M = (int)n2;
+    g.N = (int)n2;
+    g.K = nq;
+    g.gm.n = 2;
+    g.gm.dim[0] = g.gm.dim[1] = n;
+    g.gm.s0[0] = n;
+    g.gm.s0[1] = 1;
+    g.gm.s1[0] = n3;
+    g.gm.s1[1] = n;
+    g.gn.n = 2;
+    g.gn.dim[0] = g.gn.dim[1] = n;
+    g.gn.s0[0] = n;
+    g.gn.s0[1] = 1;
+    g.gn.s1[0] = n2;
+    g.gn.s1[1] = 1;
+    g.gk.n = 1;
+    g.gk.dim[0] = nq;
+    g.gk.s0[0] = n2;
+    g.gk.s1[0] = n2;
+    g.ar = 1.0;
+    g.ai = 0.0;
+    g.acc = 0;
+    g.nb = 1;
+    Program::plan_gemm(op, false);
+    CK(launch_gemm(op, B, B, tei, st));
+    CK(launch_tei_antisym(tei, n, st));
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
+  return TDCC_OK;
+}
+
+int tdcc_spectrum(const void* mu, long long nsteps, long long stride, double dt, void* Yr, void* Yi,
+                  double* energy_ev, void* stream) {
+  if (!mu || !Yr || !Yi) return fail(TDCC_ERR_ARG, "NULL argument");
+  if (nsteps < 1 || nsteps > 0x7fffffffLL || stride < 1) return fail(TDCC_ERR_ARG, "bad sizes");
+  if (!(dt > 0.0)) return fail(TDCC_ERR_ARG, "dt must be > 0");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  try {
+    void* tw = nullptr;
+    CK(cudaMallocAsync(&tw, (size_t)nsteps * 16, st));
+    const cudaError_t e = launch_spectrum(static_cast<const double2*>(mu), nsteps, stride,
+                                          static_cast<double2*>(tw), static_cast<double2*>(Yr),
+                                          static_cast<double2*>(Yi), st);
+    cudaFreeAsync(tw, st);
+    CK(e);
+    if (energy_ev)
+      for (long long j = 0; j < nsteps; ++j)
+        energy_ev[j] = (double)(j - nsteps / 2) / ((double)nsteps * dt) * (2.0 * M_PI) * 27.211;
+  } catch (const std::exception& ex) {
+    return fail(TDCC_ERR_CUDA, ex.what());
+  }
   return TDCC_OK;
 }
 

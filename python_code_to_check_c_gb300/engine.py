@@ -44,6 +44,21 @@ def to_dev(x, dtype=torch.complex128):
     return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device=dev).contiguous()
 
 
+def tei_from_df_device(B) -> torch.Tensor:
+    """<pq||rs> = sum_Q B[Q,p,r] B[Q,q,s] - B[Q,p,s] B[Q,q,r] on the device
+    (``tdcc_tei_from_df``) from the (Q, n, n) density-fitting factors; the
+    integral provider of the synthetic systems (the reference reads psi4's
+    ``mo_spin_eri``, ``CCSD_Helper.py:57-93``)."""
+    lib = _lib.load()
+    Bd = to_dev(B, torch.float64)
+    nq, n, n2 = (int(x) for x in Bd.shape)
+    if n != n2:
+        raise ValueError("B must be (Q, n, n)")
+    tei = torch.empty((n, n, n, n), dtype=torch.float64, device=Bd.device)
+    check(lib.tdcc_tei_from_df(_ptr(Bd), n, nq, _ptr(tei), _stream()), "tdcc_tei_from_df")
+    return tei
+
+
 def _ptr(x):
     return ctypes.c_void_p(x.data_ptr()) if x is not None else None
 
@@ -81,8 +96,15 @@ class CCEngine:
         self.precision = "fp64"
 
     @classmethod
-    def from_system(cls, sysm, nb: int = 1):
-        return cls(sysm.tei(), sysm.fock, sysm.mu, sysm.o, nb=nb)
+    def from_system(cls, sysm, nb: int = 1, device_integrals: bool = True):
+        """Density-fitted systems build <pq||rs> on the device
+        (``tei_from_df_device``) unless ``device_integrals`` is False; the
+        others (explicit integrals) upload them."""
+        if device_integrals and getattr(sysm, "B", None) is not None:
+            tei = tei_from_df_device(sysm.B)
+        else:
+            tei = sysm.tei()
+        return cls(tei, sysm.fock, sysm.mu, sysm.o, nb=nb)
 
     def set_fields(self, fields, pol=None):
         """Per-trajectory fields (a list of nb ``make_field`` results) and the

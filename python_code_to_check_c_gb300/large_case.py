@@ -2,7 +2,9 @@
     python -m python_code_to_check_c_gb300.large_case [--workload o24_v160] [--method CCSD]
         [--mixed-steps 10] [--fp64-steps 2]
 
-Seeded DF integrals (Q = 480 at o=24, v=160), start t1 = 0, t2 = s x MP2
+Seeded DF integrals (Q = 480 at o=24, v=160; <pq||rs> built on the device by
+tdcc_tei_from_df, its time against the host numpy build reported with
+--host-build), start t1 = 0, t2 = s x MP2
 guess, lambda = t, dt = 0.005, E = 0.002 sin(0.923 t).  The seeded
 integrals grow with n (at o=18, v=82 the MP2 correlation energy is already
 about -46 Eh and the ground-state iteration diverges), so the state is
@@ -23,8 +25,8 @@ import numpy as np
 import torch
 
 from ._lib import make_field
-from .engine import CCEngine, profile_step
-from .system import WORKLOADS, mp2_guess, synthetic_system
+from .engine import CCEngine, profile_step, tei_from_df_device
+from .system import WORKLOADS, mp2_guess_oovv, synthetic_system
 
 
 def main():
@@ -33,14 +35,26 @@ def main():
     p.add_argument("--method", default="CCSD")
     p.add_argument("--mixed-steps", type=int, default=10)
     p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--host-build", action="store_true")
     a = p.parse_args()
     t_build = time.perf_counter()
     sysm = synthetic_system(**WORKLOADS[a.workload])
-    tei = sysm.tei()
+    host_build_s = None
+    if a.host_build:
+        t_h = time.perf_counter()
+        sysm.tei()
+        host_build_s = time.perf_counter() - t_h
+    tei_from_df_device(sysm.B[:1, :2, :2])  # library load, first launch
+    torch.cuda.synchronize()
+    t_d = time.perf_counter()
+    tei = tei_from_df_device(sysm.B)
+    torch.cuda.synchronize()
+    device_build_s = time.perf_counter() - t_d
     eng = CCEngine(tei, sysm.fock, sysm.mu, sysm.o)
-    t2 = mp2_guess(tei, sysm.eps(), sysm.o).astype(np.complex128)
-    e_mp2 = 0.25 * float(np.real(np.sum(tei[: sysm.o, : sysm.o, sysm.o:, sysm.o:] * t2)))
+    oovv = tei[: sysm.o, : sysm.o, sysm.o:, sysm.o:].cpu().numpy()
     del tei
+    t2 = mp2_guess_oovv(oovv, sysm.eps(), sysm.o).astype(np.complex128)
+    e_mp2 = 0.25 * float(np.real(np.sum(oovv * t2)))
     t1 = np.zeros((sysm.o, sysm.v), dtype=np.complex128)
     t2_dev = torch.as_tensor(t2, device="cuda")
     scale = 1.0
@@ -99,7 +113,8 @@ def main():
                     for (tag, be), (ms, fl, n) in top]
     print(json.dumps({
         "workload": a.workload, "method": a.method, "o": sysm.o, "v": sysm.v, "nq": sysm.nq,
-        "build_s": build_s, "E_mp2": e_mp2, "state_scale": scale,
+        "build_s": build_s, "tei_device_build_s": device_build_s, "tei_host_build_s": host_build_s,
+        "E_mp2": e_mp2, "state_scale": scale,
         "mixed_steps_per_s": a.mixed_steps / smx, "mixed_steps": a.mixed_steps,
         "fp64_steps_per_s": a.fp64_steps / s64, "fp64_steps": a.fp64_steps,
         "mixed_over_fp64": (a.mixed_steps / smx) / (a.fp64_steps / s64), "max_dmu_au": dmu, "dmu_steps": k,

@@ -110,9 +110,14 @@ def system_from_psi4(psi4) -> System:
 
 def mp2_guess(tei: np.ndarray, eps: np.ndarray, o: int) -> np.ndarray:
     """t2 = <ij||ab> / (e_i + e_j - e_a - e_b) (``CCSD_Helper.py:102-124``)."""
+    return mp2_guess_oovv(tei[:o, :o, o:, o:], eps, o)
+
+
+def mp2_guess_oovv(oovv: np.ndarray, eps: np.ndarray, o: int) -> np.ndarray:
+    """The same from the <ij||ab> block alone."""
     eo, ev = eps[:o], eps[o:]
     d = eo[:, None, None, None] + eo[None, :, None, None] - ev[None, None, :, None] - ev[None, None, None, :]
-    return tei[:o, :o, o:, o:] / d
+    return oovv / d
 
 
 # Named workloads (sizes and generator parameters of the synthetic systems).
