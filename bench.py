@@ -151,6 +151,40 @@ def cpu_oracle_rate(sysm, method, state, budget_s=12.0, max_steps=50):
     return n / el, n, el
 
 
+_THREAD_VARS = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS")
+
+
+def _one_thread_child(workload, method, state, budget_s, max_steps, q):
+    from python_code_to_check_c_gb300.system import WORKLOADS, synthetic_system
+    sysm = synthetic_system(**WORKLOADS[workload], all_dipoles=True)
+    q.put(cpu_oracle_rate(sysm, method, state, budget_s=budget_s, max_steps=max_steps))
+
+
+def cpu_oracle_rate_one_thread(workload, method, state, budget_s=12.0, max_steps=20):
+    """The same oracle rate with one BLAS thread: a spawned process whose
+    numpy starts with the thread variables set to 1 (no GPU use there)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    saved = {k: os.environ.get(k) for k in _THREAD_VARS}
+    try:
+        for k in _THREAD_VARS:
+            os.environ[k] = "1"
+        proc = ctx.Process(target=_one_thread_child, args=(workload, method, state, budget_s, max_steps, q))
+        proc.start()
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    try:
+        res = q.get(timeout=budget_s * 10 + 300)
+    finally:
+        proc.join(timeout=60)
+    return res
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -406,10 +440,17 @@ def run_ours(args, rank, world, local_rank):
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        rate, n, el = cpu_oracle_rate(sysm, args.method, [x.cpu().numpy() for x in gs], budget_s=12.0, max_steps=20)
+        host_state = [x.cpu().numpy() for x in gs]
+        rate, n, el = cpu_oracle_rate(sysm, args.method, host_state, budget_s=12.0, max_steps=20)
         cpu = {"value": rate, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{n} RK4 steps (+dipole) of one {args.workload} trajectory in {el:.1f} s, numpy "
                          f"complex128 oracle, BLAS threads = all host cores"}
+        try:
+            r1, n1, el1 = cpu_oracle_rate_one_thread(args.workload, args.method, host_state, budget_s=12.0)
+            cpu["one_thread"] = {"value": r1, "unit": "steps/s", "cores": 1,
+                                 "sample": f"{n1} RK4 steps (+dipole) in {el1:.1f} s, same oracle, one BLAS thread"}
+        except Exception as ex:  # reported, not fatal: the all-cores figure stands
+            cpu["one_thread"] = {"unavailable": str(ex)[:200]}
     ws = eng.workspace_bytes()
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
