@@ -107,3 +107,66 @@ def test_activation_records_match_recomputation(method, checkpoint):
             assert np.abs(x - y).max() <= 1e-12 * max(np.abs(y).max(), 1e-30)
     finally:
         eng.close()
+
+
+@pytest.mark.parametrize("method", ["CCSD", "CC2"])
+def test_state_gradient_matches_torch_autograd_o6_v12(method):
+    """dJ/d(initial state) of the device reverse mode against torch autograd
+    through the oracle's reference-style einsum right-hand sides and the
+    block-frozen RK4 loop (no rounding), o=6, v=12, 6 steps."""
+    torch = pytest.importorskip("torch")
+    import math
+
+    from oracle.cc_oracle import CCOracle
+    from python_code_to_check_c_gb300._lib import make_field
+    from python_code_to_check_c_gb300.engine import CCEngine, adjoint
+    from python_code_to_check_c_gb300.system import mp2_guess, synthetic_system
+    sysm = synthetic_system(6, 12, 72, seed=612)
+    tei = sysm.tei()
+    o = sysm.o
+    rng = np.random.default_rng(13)
+    t2 = mp2_guess(tei, sysm.eps(), o) + 1e-3 * rng.standard_normal((o, o, sysm.v, sysm.v))
+    t1 = 1e-2 * (rng.standard_normal((o, sysm.v)) + 1j * rng.standard_normal((o, sysm.v)))
+    st = [t1, t2 + 0j, 0.5 * t1, 0.7 * t2 + 0j]
+    n, dt, A, w0 = 6, 0.01, 0.02, 0.923
+    w = np.cos(0.8 * dt * np.arange(1, n + 1)) * dt
+    eng = CCEngine.from_system(sysm)
+    try:
+        J, _, a = adjoint(eng, method, st, 0.0, dt, n, w, field=make_field("sin", A, w0), checkpoint=4,
+                          want_state_grad=True)
+        a = [x.detach().cpu().numpy() for x in a]
+    finally:
+        eng.close()
+
+    mu_z = torch.as_tensor(sysm.mu[2]).to(torch.complex128)
+    orc = CCOracle(torch.as_tensor(tei).to(torch.complex128), o)
+    F = torch.as_tensor(sysm.fock).to(torch.complex128)
+    x = [torch.as_tensor(s).clone().requires_grad_(True) for s in st]
+    Vt = lambda t: -(A * math.sin(w0 * t)) * mu_z  # noqa: E731
+
+    def dipole(t1, t2, l1, l2):
+        rho = torch.cat([torch.cat([orc.Dij(t1, t2, l1, l2), l1], 1),
+                         torch.cat([orc.Dai(t1, t2, l1, l2), orc.Dab(t1, t2, l1, l2)], 1)], 0)
+        return torch.sum(mu_z * rho)
+
+    t1, t2, l1, l2 = x
+    t = 0.0
+    Jt = 0.0
+    for k in range(n):
+        t += dt
+        d1 = -1j * orc.ft1(t, dt, t1, t2, F, Vt)
+        if method == "CCSD":
+            d2 = -1j * orc.ft2(t, dt, t1, t2, F, Vt)
+            e1 = 1j * orc.fL1(t, dt, t1, t2, l1, l2, F, Vt)
+            e2 = 1j * orc.fL2(t, dt, t1, t2, l1, l2, F, Vt)
+        else:
+            d2 = -1j * orc.ft2_CC2(t, dt, t1, t2, F, Vt)
+            e1 = 1j * orc.fL1_CC2(t, dt, t1, t2, l1, l2, F, Vt)
+            e2 = 1j * orc.fL2_CC2(t, dt, t1, t2, l1, l2, F, Vt)
+        t1, t2, l1, l2 = t1 + d1, t2 + d2, l1 + e1, l2 + e2
+        Jt = Jt + w[k] * dipole(t1, t2, l1, l2).real
+    assert abs(float(Jt.detach()) - float(J[0])) <= 1e-12 * max(1.0, abs(float(J[0])))
+    grads = torch.autograd.grad(Jt, x)
+    for ours, g in zip(a, grads):
+        ref = np.conj(g.numpy())  # torch's gradient of a real J is dJ/dRe z + i dJ/dIm z
+        assert np.abs(ours - ref).max() <= 1e-10 * np.abs(ref).max(), np.abs(ours - ref).max() / np.abs(ref).max()
