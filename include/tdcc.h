@@ -139,11 +139,12 @@ int tdcc_ground_state(tdcc_system s, int method, int mode, void* t1, void* t2, v
                       const double* eps, int maxsize, int maxiter, double e_min, double r_tol,
                       double* energy, int* niter, void* stream);
 
-/* Mixed mode routing: contractions with at least min_macs multiply-adds and
-   a contracted extent K >= min_k run on the tensor cores (defaults 2^18 and
-   32); the rest stay FP64.  (0, 1) sends every contraction to the tensor
-   cores, which tests use at small sizes.                                  */
-int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k);
+/* Mixed mode routing: contractions with at least min_macs multiply-adds, a
+   contracted extent K >= min_k and output extents M, N >= min_mn (per
+   launch, trajectories folded in) run on the tensor cores (defaults 2^18,
+   32, 1); the rest stay FP64.  (0, 1, 1) sends every contraction to the
+   tensor cores, which tests use at small sizes.                           */
+int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k, int min_mn);
 
 /* Workspace buffer sharing (no counterpart in the reference): a program whose
    workspace slots add up to more than min_bytes lets slots with disjoint

@@ -100,10 +100,16 @@ long long workspace_estimate(const Program& p) {
   return b;
 }
 
-// contractions with at least this many multiply-adds (and K >= 64) use the
-// tensor-core slice products in the mixed-precision mode
+// contractions with at least this many multiply-adds, K >= kTcMinK and both
+// output extents (per launch: M and N of the batched GEMM) >= kTcMinMN use
+// the tensor-core slice products in the mixed-precision mode.  No output
+// limit by default: contractions with 10 x 10 or 1 x N outputs pack mostly
+// padding and take longer alone than in FP64, but the step runs its ops
+// concurrently and the FP64 pipe is the shared bottleneck there (o=10, v=38:
+// a limit of 16 cost 14 % with 24 trajectories, 8 % with one).
 constexpr long long kTcMinMacs = 1LL << 18;
 constexpr int kTcMinK = 32;
+constexpr int kTcMinMN = 1;
 
 }  // namespace tdcc
 
@@ -119,6 +125,7 @@ struct tdcc_system_s {
   int slices = 5;
   long long tc_min_macs = kTcMinMacs;  // tensor-core routing policy
   int tc_min_k = kTcMinK;
+  int tc_min_mn = kTcMinMN;
   int device = 0;
   int nb = 1;                       // trajectories advanced together
   bool share_mem = true;            // workspace slots with disjoint lifetimes share memory (off once
@@ -216,7 +223,7 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
   else
     build_l2_cc2(p, p.ones("ones_v", s->dims.v));
   p.batch(s->nb);
-  p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
+  p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
   if (s->share_mem && workspace_estimate(p) > (s->share_min < 0 ? kShareMinBytes : s->share_min)) p.plan_memory();
@@ -235,7 +242,7 @@ ProgInst& get_density(tdcc_system s) {
   pi->prog = std::make_unique<Program>(s->dims, "density");
   build_density(*pi->prog, s->n_mu);
   pi->prog->batch(s->nb);
-  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
+  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn);
   pi->prog->analyse({});
   if (s->share_mem && workspace_estimate(*pi->prog) > (s->share_min < 0 ? kShareMinBytes : s->share_min))
     pi->prog->plan_memory();
@@ -270,7 +277,7 @@ ProgInst& get_adj(tdcc_system s, int method, int block) {
   auto pi = std::make_unique<ProgInst>();
   pi->prog = std::make_unique<Program>(s->dims, "adj");
   build_adjoint(f, *pi->prog, s->adj_of[method][block]);
-  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k);
+  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn);
   pi->nfwd = f.slots.size();
   pi->bases.assign(pi->prog->slots.size(), nullptr);
   pi->bytes = pi->prog->allocate(pi->bases, pi->owned, pi->nfwd, true);
@@ -658,13 +665,15 @@ int tdcc_set_adjoint_store(tdcc_system s, int mode) {
   return TDCC_OK;
 }
 
-int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k) {
+int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k, int min_mn) {
   if (!s) return fail(TDCC_ERR_ARG, "null system");
-  if (min_macs < 0 || min_k < 1) return fail(TDCC_ERR_ARG, "min_macs >= 0 and min_k >= 1 required");
-  if (min_macs == s->tc_min_macs && min_k == s->tc_min_k) return TDCC_OK;
+  if (min_macs < 0 || min_k < 1 || min_mn < 1)
+    return fail(TDCC_ERR_ARG, "min_macs >= 0, min_k >= 1 and min_mn >= 1 required");
+  if (min_macs == s->tc_min_macs && min_k == s->tc_min_k && min_mn == s->tc_min_mn) return TDCC_OK;
   reset_programs(s);
   s->tc_min_macs = min_macs;
   s->tc_min_k = min_k;
+  s->tc_min_mn = min_mn;
   return TDCC_OK;
 }
 

@@ -331,9 +331,9 @@ class Program {
 
   // mixed precision: which GEMMs go to the tensor-core backend
   // (before analyse/allocate) rewrites every contraction with at least
-  // `min_macs` multiply-adds and K >= min_k into pack A, pack B and a
+  // `min_macs` multiply-adds, K >= min_k and M, N >= min_mn into pack A, pack B and a
   // tensor-core slice product with `slices` BF16 slices per operand
-  void select_backend(int prec_mode, long long min_macs, int slices, int min_k);
+  void select_backend(int prec_mode, long long min_macs, int slices, int min_k, int min_mn);
   int err_slot = -1;  // U8 slot holding the tensor-core kernels' error flag
 };
 

@@ -873,7 +873,7 @@ cudaError_t Program::run_dag(const std::vector<void*>& bases, cudaStream_t st, P
 
 static long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
 
-void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k) {
+void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k, int min_mn) {
   if (prec_mode != 1) return;
   if (S < 1 || S > 6) throw std::runtime_error("slices must be 1..6");
   constexpr int BM = 128, BN = 64, BK = 64;  // tensor-core tile (gemm_tc.h)
@@ -908,7 +908,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
       continue;
     }
     const long long M = op.g.M, N = op.g.N, K = op.g.K;
-    if (M * N * K * std::max(op.g.nb, 1) < min_macs || K < min_k) {
+    if (M * N * K * std::max(op.g.nb, 1) < min_macs || K < min_k || std::min(M, N) < min_mn) {
       push_op(op);
       continue;
     }

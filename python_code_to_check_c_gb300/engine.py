@@ -139,9 +139,10 @@ class CCEngine:
         check(self.lib.tdcc_set_precision(self.handle, m, int(slices)), "tdcc_set_precision")
         self.precision = mode
 
-    def set_tc_policy(self, min_macs: int = 1 << 18, min_k: int = 32):
+    def set_tc_policy(self, min_macs: int = 1 << 18, min_k: int = 32, min_mn: int = 1):
         """Which contractions the mixed mode sends to the tensor cores."""
-        check(self.lib.tdcc_set_tc_policy(self.handle, int(min_macs), int(min_k)), "tdcc_set_tc_policy")
+        check(self.lib.tdcc_set_tc_policy(self.handle, int(min_macs), int(min_k), int(min_mn)),
+              "tdcc_set_tc_policy")
 
     def set_memory_sharing(self, min_bytes: int = -1):
         """Workspace buffer sharing above min_bytes per program (-1: default

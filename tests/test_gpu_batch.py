@@ -60,7 +60,7 @@ def test_batched_propagation_equals_single_runs(method, precision):
     eb = CCEngine.from_system(sysm, nb=NB)
     if precision == "mixed":
         eb.set_precision("mixed", 5)
-        eb.set_tc_policy(0, 1)
+        eb.set_tc_policy(0, 1, 1)
     eb.set_fields(fields, pol)
     batch_state = [np.stack([s[k] for s in states]) for k in range(4)]
     fin_b, traj_b = eb.propagate(method, batch_state, 0.0, dt, nsteps, None, precs=15)
@@ -71,7 +71,7 @@ def test_batched_propagation_equals_single_runs(method, precision):
         es = CCEngine.from_system(sysm)
         if precision == "mixed":
             es.set_precision("mixed", 5)
-            es.set_tc_policy(0, 1)
+            es.set_tc_policy(0, 1, 1)
         es.set_fields([fields[z]], [pol[z]])
         fin_s, traj_s = es.propagate(method, states[z], 0.0, dt, nsteps, None, precs=15)
         tol = 1e-12 if precision == "fp64" else 1e-10

@@ -76,7 +76,7 @@ def test_residual_tolerance_and_mixed_precision():
         E1, n1, _, _ = eng.ground_state("CCSD", 0, t1, t2, maxiter=60, E_min=0.0, r_tol=1e-11)
         assert abs(E1 - E0) < 1e-10 and n1 <= 60
         eng.set_precision("mixed", 5)
-        eng.set_tc_policy(0, 1)
+        eng.set_tc_policy(0, 1, 1)
         E2, _, _, _ = eng.ground_state("CCSD", 0, t1, t2, maxiter=40, E_min=1e-15)
         eng.check_errors()
         assert abs(E2 - E0) < 1e-10

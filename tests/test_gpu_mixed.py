@@ -27,7 +27,7 @@ def case(request):
     d, sysm = load(request.param)
     eng = CCEngine.from_system(sysm)
     eng.set_precision("mixed", 5)
-    eng.set_tc_policy(0, 1)  # every contraction on the tensor cores at these small sizes
+    eng.set_tc_policy(0, 1, 1)  # every contraction on the tensor cores at these small sizes
     yield d, sysm, eng
     eng.close()
 
@@ -52,7 +52,7 @@ def test_slices_control_the_error():
     d, sysm = load("golden_o6_v10.npz")
     eng = CCEngine.from_system(sysm)
     errs = []
-    eng.set_tc_policy(0, 1)
+    eng.set_tc_policy(0, 1, 1)
     try:
         for S in (3, 4, 5, 6):
             eng.set_precision("mixed", S)

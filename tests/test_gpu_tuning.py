@@ -21,7 +21,7 @@ def _run(method, prec, nb, sharing=None, tune=False, steps=8):
     try:
         if prec == "mixed":
             eng.set_precision("mixed", 5)
-            eng.set_tc_policy(0, 1)
+            eng.set_tc_policy(0, 1, 1)
         if sharing is not None:
             eng.set_memory_sharing(sharing)
         st = [d["t1"] + 0j, d["t2"] + 0j, d["l1"] + 0j, d["l2"] + 0j]
