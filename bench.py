@@ -45,9 +45,11 @@ AMPS = (0.001, 0.002, 0.005, 0.01)
 W0S = (0.5, 0.923)
 POLS = (0, 1, 2)
 REF_TRAJ = (2, 0.002, 0.923)  # the single-trajectory configuration (z, A, w0)
-# DRAM bytes per launch of the step's dominant kernels, from one ncu capture of the same
-# contraction at 8 trajectories scaled by 3 (traffic grows with the trajectory count)
-TRAFFIC_PER_LAUNCH = {("ccsd_t2:mnij,mnab->ijab", 24): 3 * (51.46e6 + 0.55e6)}
+# DRAM bytes (read + write) per launch of the step's dominant slice products, from one
+# single-pass ncu capture (dram__bytes_read.sum, dram__bytes_write.sum) of the T2 program at
+# 24 trajectories: the ladder with the shared integral operand, and the batched Wmnij product
+TRAFFIC_PER_LAUNCH = {("ccsd_t2:abef,ijef->ijab", 24): 150.44e6 + 36.12e6,
+                      ("ccsd_t2:mnij,mnab->ijab", 24): 154.17e6 + 28.77e6}
 
 
 def parse():
@@ -428,7 +430,8 @@ def run_ours(args, rank, world, local_rank):
         roof = {"bound": "hbm", "unit": "GB/s", "peak_source": "measured HBM copy (MEASURED_PEAKS.json)"}
     traffic = TRAFFIC_PER_LAUNCH.get((tag, nb))
     roof.update({"kernel": tag, "achieved": achieved, "peak": peak, "frac": achieved / peak,
-                 "traffic": traffic, "traffic_source": "ncu capture at 8 trajectories x 3" if traffic else None,
+                 "traffic": traffic,
+                 "traffic_source": "ncu capture of the same contraction at 24 trajectories" if traffic else None,
                  "launches_per_step": dom["n"], "share_of_step": dom["ms"] / tot,
                  "avg_launch_ms": dom["ms"] / dom["n"]})
     top = sorted(by.items(), key=lambda kv: -kv[1]["ms"])[:6]

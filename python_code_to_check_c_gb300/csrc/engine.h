@@ -155,6 +155,7 @@ struct TcArgs {
   int rowsA_pad, rowsB_pad; // packed rows per batch
   int nb, nsplit;           // blockIdx.z = batch * nsplit + split
   int variant;              // 0: 64-wide tile, one CTA per SM; 1: 32-wide, two per SM
+  int m_fast;               // launch order: M tiles fastest (set by the launcher)
   int bat_a, bat_b;         // A / B packed per batch (else shared by all batches)
   long long bsC;            // output batch stride in elements
   int kblocks, kb_per_split;

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = sh->tmem;
 
-  const int mt = blockIdx.y, nt = blockIdx.x;
+  const int mt = g.m_fast ? blockIdx.x : blockIdx.y, nt = g.m_fast ? blockIdx.y : blockIdx.x;
   const int zb = blockIdx.z / g.nsplit;                 // batch
   const int kb0 = (blockIdx.z - zb * g.nsplit) * g.kb_per_split;
   const int rowA0 = (g.bat_a ? zb * g.rowsA_pad : 0);  // packed-row origin of this batch
@@ -738,7 +738,13 @@ static cudaError_t launch_variant(const TcArgs& a0, const void* packA, const voi
   if (a.rowsB_pad % C::BN != 0) return cudaErrorInvalidValue;
   const CUtensorMap ma = slice_map(packA, a.S, (a.bat_a ? a.nb : 1) * a.rowsA_pad, a.kblocks * TC_BK, TC_BM);
   const CUtensorMap mb = slice_map(packB, a.S, (a.bat_b ? a.nb : 1) * a.rowsB_pad, a.kblocks * TC_BK, C::BN);
-  dim3 grid(a.rowsB_pad / C::BN, a.rowsA_pad / TC_BM, (unsigned)((long long)a.nb * a.nsplit));
+  // CTA order: the tiles of the smaller operand side vary fastest, so that
+  // side stays in L2 while each tile of the larger side is read from DRAM
+  // once (the N-fastest order re-read the 69 MB of packed amplitudes of the
+  // 24-trajectory ladder for each of its 12 M strips: 430 MB per launch)
+  const unsigned mtiles = (unsigned)(a.rowsA_pad / TC_BM), ntiles = (unsigned)(a.rowsB_pad / C::BN);
+  a.m_fast = (a.rowsA_pad < a.rowsB_pad && ntiles <= 65535u) ? 1 : 0;
+  dim3 grid(a.m_fast ? mtiles : ntiles, a.m_fast ? ntiles : mtiles, (unsigned)((long long)a.nb * a.nsplit));
   if (a.ac && a.bc)
     ozaki_kernel<true, true, C><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
   else if (a.ac)
