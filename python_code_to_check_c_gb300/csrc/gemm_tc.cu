@@ -12,8 +12,11 @@
 // Products (ozaki_kernel): for every pair (s, t) with s + t <= S + 1 the
 // slice product A_s B_t^T is accumulated by tcgen05.mma (kind::f16, BF16
 // inputs, FP32 accumulate in TMEM) into the accumulator of its level
-// L = s + t.  |q_s q_t| <= 2^14, so FP32 sums of up to 1024 products are
-// exact; after every 1024-wide K chunk the epilogue warps drain the TMEM
+// L = s + t.  With |q_1| <= 128 and |q_s| <= 64 the products of one level
+// at one K index add up to at most 2^14 + 2^13 + 2^13 = 2^15 in magnitude
+// (level 7 of S = 6; 2^14 + 2^13 + 2^12 for level 6), so the FP32 level sums
+// over a 512-wide K chunk stay within 2^24 and are exact integers; after
+// every chunk the epilogue warps drain the TMEM
 // accumulators into FP64 registers with their 2^(-7L) weights.  The final
 // value is scaled back by 2^(e_row + e_col); real/imaginary rows of complex
 // operands are combined with a lane-pair shuffle and written through the

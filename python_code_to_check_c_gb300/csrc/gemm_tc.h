@@ -11,7 +11,7 @@ namespace tdcc {
 constexpr int TC_BM = 128;                   // UMMA M (rows of A per CTA)
 constexpr int TC_BN = 64;                    // packed B rows are padded to this (both variants)
 constexpr int TC_BK = 64;                    // K per TMA box (128 B of BF16)
-constexpr int TC_CHUNK_KB = 16;              // 1024-wide K chunks (exact FP32 sums)
+constexpr int TC_CHUNK_KB = 8;               // 512-wide K chunks (exact FP32 level sums)
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
 constexpr int TC_MAX_SLICES = 6;
 
