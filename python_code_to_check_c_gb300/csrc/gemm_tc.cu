@@ -91,32 +91,30 @@ __device__ __forceinline__ unsigned long long fixed_point(double x, int e, int n
 // bits into S signed 7-bit digits (|q_s| <= 127, exact in BF16):
 //   x 2^-e ~= sum_s q_s 2^(-7s).
 // The real and imaginary rows share e, so that the slice-product epilogue
-// combines re*re - im*im and re*im + im*re exactly in integers.  Padding rows
-// and columns are written as zero (exponent entry 0).
+// combines re*re - im*im and re*im + im*re exactly in integers.  K padding
+// is written as zero; padding rows (up to the tile multiple of each batch)
+// are not written at all: they only feed accumulator rows (A) or columns (B)
+// that the product kernel never stores, and their exponent entries only
+// scale those values, so whatever the buffer holds there is harmless.
 __global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
   const int per = p.cplx ? 2 : 1;
-  const int rl_pad = p.rows_pad / per;  // logical rows per batch, padding included
-  const int z = blockIdx.x / rl_pad, m = blockIdx.x - z * rl_pad;
-  const bool live = m < p.rows;
+  const int z = blockIdx.x / p.rows, m = blockIdx.x - z * p.rows;  // one block per live row
   long long ro = 0;
-  if (live) {
-    decomp_tc(p.gr, m, ro);
-    ro += z * p.bs;
-  }
+  decomp_tc(p.gr, m, ro);
+  ro += z * p.bs;
   const unsigned long long* bits = static_cast<const unsigned long long*>(p.src);
   const double* src = static_cast<const double*>(p.src);
   constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
   unsigned long long mx = 0;
-  if (live)
-    for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
-      long long ko;
-      decomp_tc(p.gk, k, ko);
-      const long long e = ro + ko;
-      if (p.cplx)
-        mx = max(mx, max(bits[2 * e] & kAbs, bits[2 * e + 1] & kAbs));
-      else
-        mx = max(mx, bits[e] & kAbs);
-    }
+  for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
+    long long ko;
+    decomp_tc(p.gk, k, ko);
+    const long long e = ro + ko;
+    if (p.cplx)
+      mx = max(mx, max(bits[2 * e] & kAbs, bits[2 * e + 1] & kAbs));
+    else
+      mx = max(mx, bits[e] & kAbs);
+  }
   for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
   __shared__ unsigned long long wmax[8];
   if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
@@ -136,7 +134,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
   const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
   for (int k = threadIdx.x; k < p.K_pad; k += blockDim.x) {
     double x[2] = {0.0, 0.0};
-    if (live && k < p.K) {
+    if (k < p.K) {
       long long ko;
       decomp_tc(p.gk, k, ko);
       const long long el = ro + ko;
@@ -696,8 +694,9 @@ static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, i
 }
 
 cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
-  if (p.nb < 1 || p.rows_pad % (p.cplx ? 2 : 1) != 0) return cudaErrorInvalidValue;
-  const long long blocks = (long long)p.nb * (p.rows_pad / (p.cplx ? 2 : 1));
+  if (p.nb < 1 || p.rows < 1 || p.rows_pad % (p.cplx ? 2 : 1) != 0 || p.rows * (p.cplx ? 2 : 1) > p.rows_pad)
+    return cudaErrorInvalidValue;
+  const long long blocks = (long long)p.nb * p.rows;
   if (blocks > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;
   const int threads = p.K_pad >= 256 ? 256 : ((p.K_pad + 31) / 32) * 32;
   pack_kernel<<<(unsigned)blocks, threads, 0, st>>>(p);
