@@ -146,6 +146,12 @@ int tdcc_ground_state(tdcc_system s, int method, int mode, void* t1, void* t2, v
    tensor cores, which tests use at small sizes.                           */
 int tdcc_set_tc_policy(tdcc_system s, long long min_macs, int min_k, int min_mn);
 
+/* Mixed mode, contractions the tensor cores leave out: those with K <= max_k
+   and at least min_macs multiply-adds run as the same exact BF16-digit slice
+   products on the FP32 pipe (defaults 64 and 2^14; max_k = 0 keeps them
+   FP64).  GB300's FP64 pipe is narrow and shared with the elementwise ops. */
+int tdcc_set_simt_policy(tdcc_system s, int max_k, long long min_macs);
+
 /* Workspace buffer sharing (no counterpart in the reference): a program whose
    workspace slots add up to more than min_bytes lets slots with disjoint
    lifetimes within one phase share memory (fewer bytes, some ops ordered

@@ -67,6 +67,7 @@ SIGNATURES = {
     "tdcc_workspace_bytes": (_ll, [_vp]),
     "tdcc_check_errors": (_i, [_vp]),
     "tdcc_set_tc_policy": (_i, [_vp, _ll, _i, _i]),
+    "tdcc_set_simt_policy": (_i, [_vp, _i, _ll]),
     "tdcc_set_memory_sharing": (_i, [_vp, _ll]),
     "tdcc_set_adjoint_store": (_i, [_vp, _i]),
     "tdcc_tei_from_df": (_i, [_vp, _i, _i, _vp, _vp]),

@@ -110,6 +110,10 @@ long long workspace_estimate(const Program& p) {
 constexpr long long kTcMinMacs = 1LL << 18;
 constexpr int kTcMinK = 32;
 constexpr int kTcMinMN = 1;
+// contractions the tensor cores leave out with K <= 64 and at least 2^14
+// multiply-adds run as slice products on the FP32 pipe (mixed mode)
+constexpr int kSimtMaxKDefault = 64;
+constexpr long long kSimtMinMacs = 1LL << 14;
 
 }  // namespace tdcc
 
@@ -126,6 +130,8 @@ struct tdcc_system_s {
   long long tc_min_macs = kTcMinMacs;  // tensor-core routing policy
   int tc_min_k = kTcMinK;
   int tc_min_mn = kTcMinMN;
+  int simt_max_k = kSimtMaxKDefault;   // short contractions on the FP32 pipe (mixed mode)
+  long long simt_min_macs = kSimtMinMacs;
   int device = 0;
   int nb = 1;                       // trajectories advanced together
   bool share_mem = true;            // workspace slots with disjoint lifetimes share memory (off once
@@ -223,7 +229,8 @@ ProgInst& get_rhs(tdcc_system s, int method, int block) {
   else
     build_l2_cc2(p, p.ones("ones_v", s->dims.v));
   p.batch(s->nb);
-  p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn);
+  p.select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn, s->simt_max_k,
+                          s->simt_min_macs);
   // the block's own amplitude and the dressed Fock vary across RK4 stages
   p.analyse({S_T1 + block, S_F});
   if (s->share_mem && workspace_estimate(p) > (s->share_min < 0 ? kShareMinBytes : s->share_min)) p.plan_memory();
@@ -242,7 +249,8 @@ ProgInst& get_density(tdcc_system s) {
   pi->prog = std::make_unique<Program>(s->dims, "density");
   build_density(*pi->prog, s->n_mu);
   pi->prog->batch(s->nb);
-  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn);
+  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn, s->simt_max_k,
+                          s->simt_min_macs);
   pi->prog->analyse({});
   if (s->share_mem && workspace_estimate(*pi->prog) > (s->share_min < 0 ? kShareMinBytes : s->share_min))
     pi->prog->plan_memory();
@@ -277,7 +285,8 @@ ProgInst& get_adj(tdcc_system s, int method, int block) {
   auto pi = std::make_unique<ProgInst>();
   pi->prog = std::make_unique<Program>(s->dims, "adj");
   build_adjoint(f, *pi->prog, s->adj_of[method][block]);
-  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn);
+  pi->prog->select_backend(s->prec_mode, s->tc_min_macs, s->slices, s->tc_min_k, s->tc_min_mn, s->simt_max_k,
+                          s->simt_min_macs);
   pi->nfwd = f.slots.size();
   pi->bases.assign(pi->prog->slots.size(), nullptr);
   pi->bytes = pi->prog->allocate(pi->bases, pi->owned, pi->nfwd, true);
@@ -662,6 +671,16 @@ int tdcc_set_adjoint_store(tdcc_system s, int mode) {
   if (!s) return fail(TDCC_ERR_ARG, "null system");
   if (mode < -1 || mode > 1) return fail(TDCC_ERR_ARG, "mode must be -1, 0 or 1");
   s->adj_store = mode;
+  return TDCC_OK;
+}
+
+int tdcc_set_simt_policy(tdcc_system s, int max_k, long long min_macs) {
+  if (!s) return fail(TDCC_ERR_ARG, "null system");
+  if (max_k < 0 || max_k > 64 || min_macs < 0) return fail(TDCC_ERR_ARG, "0 <= max_k <= 64 and min_macs >= 0 required");
+  if (max_k == s->simt_max_k && min_macs == s->simt_min_macs) return TDCC_OK;
+  reset_programs(s);
+  s->simt_max_k = max_k;
+  s->simt_min_macs = min_macs;
   return TDCC_OK;
 }
 
@@ -1158,7 +1177,7 @@ int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, con
       ProgInst& pi = *pip;
       pi.check_bound();
       for (Op& op : pi.prog->ops) {
-        if (op.kind == OP_GEMM) {
+        if (op.kind == OP_GEMM && op.backend == GB_FP64) {
           const double t_cur = time_op(pi, op);
           double best = t_cur;
           Op best_op = op;

@@ -173,7 +173,9 @@ struct TcArgs {
   int* err;
 };
 
-enum GemmBackend { GB_FP64 = 0, GB_TC = 1 };
+// GB_SIMT: exact BF16-digit slice products on the FP32 pipe for short
+// contractions of the mixed mode (gemm_tc.cu)
+enum GemmBackend { GB_FP64 = 0, GB_TC = 1, GB_SIMT = 2 };
 
 struct Op {
   OpKind kind;
@@ -334,7 +336,10 @@ class Program {
   // (before analyse/allocate) rewrites every contraction with at least
   // `min_macs` multiply-adds, K >= min_k and M, N >= min_mn into pack A, pack B and a
   // tensor-core slice product with `slices` BF16 slices per operand
-  void select_backend(int prec_mode, long long min_macs, int slices, int min_k, int min_mn);
+  // contractions left out with K <= simt_max_k and at least simt_min_macs
+  // multiply-adds run as slice products on the FP32 pipe (GB_SIMT)
+  void select_backend(int prec_mode, long long min_macs, int slices, int min_k, int min_mn, int simt_max_k,
+                      long long simt_min_macs);
   int err_slot = -1;  // U8 slot holding the tensor-core kernels' error flag
 };
 
@@ -361,6 +366,8 @@ bool tile_fits(int tile, long long M);  // the M tiles fit the launch grid
 cudaError_t launch_gemm(const Op& op, const void* A, const void* B, void* C, cudaStream_t st);
 cudaError_t launch_pack(const PackArgs& p, cudaStream_t st);
 cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st);
+bool simt_slices_supported(int K, int S);
+cudaError_t launch_simt_slices(const Op& op, const void* A, const void* B, void* C, cudaStream_t st);
 bool tc_available();
 cudaError_t launch_add(const AddArgs& a, cudaStream_t st);
 cudaError_t launch_reduce(const ReduceArgs& r, cudaStream_t st);

@@ -649,6 +649,286 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
 }
 
 // ---------------------------------------------------------------------------
+// Short contractions (K <= 64) of the mixed mode on the FP32 pipe: the same
+// exact slice products as the tensor-core path, without packing.  One output
+// tile per block: the block takes the binary exponents of its rows of A and
+// columns of B over all of K (real and imaginary parts share one), cuts K
+// chunks of both into S signed 7-bit digits in shared memory, and every
+// thread accumulates the levels L = s + t of its 4 outputs with FP32 FMAs.  A complex level sum grows by at most
+// 2 (2^14 + 2^13 + 2^13) = 2^16 per K index, so up to K = 64 every partial
+// sum is an integer below 2^22, exact in FP32.  The epilogue recombines the
+// levels in int64 and converts with the exponents, as the tensor-core drain
+// does.  GB300's FP64 pipe runs about 2 FMA per clock per SM, its FP32 pipe
+// 128: 60 FP32 FMAs per complex multiply-add still finish 4x sooner than 4
+// FP64 ones, and the FP64 pipe stays free for the elementwise ops.
+// ---------------------------------------------------------------------------
+constexpr int kSimtMaxK = 64;
+
+// Tile BM x BN (32 x 32, 16 x 64 or 64 x 16), 256 threads on a 16 x 16 grid,
+// 4 outputs each: rows ty + 16 i, columns tx + 16 j.  Digits in shared memory
+// per K index and row: S x (2 if complex) floats, contiguous, read as float2.
+template <bool AC, bool BC, bool CC, int S, int BM, int BN>
+__global__ void __launch_bounds__(256, 2) simt_slices_kernel(const GemmArgs g, int alpha_pow2, int alpha_e,
+                                                             int alpha_neg) {
+  constexpr int PA = AC ? 2 : 1, PB = BC ? 2 : 1;
+  constexpr int SPA = (S * PA + 1) / 2 * 2, SPB = (S * PB + 1) / 2 * 2;  // floats per row, even
+  constexpr int MI = BM / 16, NJ = BN / 16;
+  static_assert(MI * NJ == 4, "four outputs per thread");
+  constexpr int KC = (BM > 32 || BN > 32) ? 8 : 16;  // K chunk (static shared memory <= 48 KB)
+  __shared__ __align__(8) float sa[KC][BM][SPA];
+  __shared__ __align__(8) float sb[KC][BN][SPB];
+  __shared__ long long aoff[BM], boff[BN], coffm[BM], coffn[BN];
+  __shared__ long long kofa[kSimtMaxK], kofb[kSimtMaxK];
+  __shared__ int ea[BM], eb[BN];
+  const int tid = threadIdx.x;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN, zb = blockIdx.z;
+  const double* A = static_cast<const double*>(g.A) + (size_t)zb * g.bsA * PA;
+  const double* B = static_cast<const double*>(g.B) + (size_t)zb * g.bsB * PB;
+  auto dec = [](const ModeGroup& gr, int l, long long& o0, long long& o1) {
+    o0 = 0;
+    o1 = 0;
+    for (int q = kMaxModes - 1; q >= 0; --q)
+      if (q < gr.n) {
+        const int r = l % gr.dim[q];
+        l /= gr.dim[q];
+        o0 += (long long)r * gr.s0[q];
+        o1 += (long long)r * gr.s1[q];
+      }
+  };
+  if (tid < BM) {
+    long long o0 = -1, o1 = -1;
+    if (m0 + tid < g.M) dec(g.gm, m0 + tid, o0, o1);
+    aoff[tid] = o0;
+    coffm[tid] = o1;
+  } else if (tid < BM + BN) {
+    const int c = tid - BM;
+    long long o0 = -1, o1 = -1;
+    if (n0 + c < g.N) dec(g.gn, n0 + c, o0, o1);
+    boff[c] = o0;
+    coffn[c] = o1;
+  } else if (tid < BM + BN + g.K) {
+    const int k = tid - BM - BN;
+    dec(g.gk, k, kofa[k], kofb[k]);
+  }
+  __syncthreads();
+  // exponents of the tile's rows of A and columns of B over all of K: every
+  // thread takes elements (row, k) with independent loads, the maxima of the
+  // bit patterns (the order of |x| for finite doubles) meet in shared memory
+  constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
+  __shared__ unsigned long long rmax[BM + BN];
+  if (tid < BM + BN) rmax[tid] = 0ull;
+  __syncthreads();
+  for (int idx = tid; idx < (BM + BN) * g.K; idx += blockDim.x) {
+    const int r = idx % (BM + BN), k = idx / (BM + BN);
+    const bool isA = r < BM;
+    const long long base = isA ? aoff[r] : boff[r - BM];
+    if (base < 0) continue;
+    const unsigned long long* bits =
+        reinterpret_cast<const unsigned long long*>(isA ? static_cast<const void*>(A) : static_cast<const void*>(B));
+    const int per = isA ? PA : PB;
+    const long long el = base + (isA ? kofa[k] : kofb[k]);
+    unsigned long long v = bits[per * el] & kAbs;
+    if (per == 2) v = max(v, bits[2 * el + 1] & kAbs);
+    if (v) atomicMax(&rmax[r], v);
+  }
+  __syncthreads();
+  if (tid < BM + BN) {
+    const unsigned long long mx = rmax[tid];
+    const int E = (int)(mx >> 52);
+    const int e = mx != 0 ? (E > 0 ? E - 1022 : -1022) : 0;
+    if (tid < BM)
+      ea[tid] = e;
+    else
+      eb[tid - BM] = e;
+  }
+  __syncthreads();
+  const int tx = tid % 16, ty = tid / 16;
+  float acc[MI][NJ][S][2];
+#pragma unroll
+  for (int i = 0; i < MI; ++i)
+#pragma unroll
+    for (int j = 0; j < NJ; ++j)
+#pragma unroll
+      for (int L = 0; L < S; ++L) acc[i][j][L][0] = acc[i][j][L][1] = 0.f;
+  constexpr int nbits = 7 * S;
+  for (int kc = 0; kc < g.K; kc += KC) {
+    // digits of the chunk: BM rows x KC of A, KC x BN columns of B
+    for (int idx = tid; idx < (BM + BN) * KC; idx += blockDim.x) {
+      const bool isA = idx < BM * KC;
+      const int id2 = isA ? idx : idx - BM * KC;
+      const int nr = isA ? BM : BN;
+      const int r = id2 % nr, kk = id2 / nr, k = kc + kk;
+      const long long base = isA ? aoff[r] : boff[r];
+      const int per = isA ? PA : PB;
+      double x[2] = {0.0, 0.0};
+      if (base >= 0 && k < g.K) {
+        const double* src = isA ? A : B;
+        const long long el = base + (isA ? kofa[k] : kofb[k]);
+        x[0] = src[per * el];
+        if (per == 2) x[1] = src[2 * el + 1];
+      }
+      const int e = isA ? ea[r] : eb[r];
+      float* dst = isA ? &sa[kk][r][0] : &sb[kk][r][0];
+      for (int part = 0; part < per; ++part) {
+        const unsigned long long f = fixed_point(x[part], e, nbits);
+        const bool neg = x[part] < 0.0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const int q = (int)((f >> (7 * (S - 1 - s))) & 127ull);
+          dst[s * per + part] = (float)(neg ? -q : q);
+        }
+      }
+    }
+    __syncthreads();
+    const int kn = min(KC, g.K - kc);
+    for (int kk = 0; kk < kn; ++kk) {
+      float a[MI][SPA], b[NJ][SPB];
+#pragma unroll
+      for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int q = 0; q < SPA / 2; ++q) {
+          const float2 v = *reinterpret_cast<const float2*>(&sa[kk][ty + 16 * i][2 * q]);
+          a[i][2 * q] = v.x;
+          a[i][2 * q + 1] = v.y;
+        }
+#pragma unroll
+      for (int j = 0; j < NJ; ++j)
+#pragma unroll
+        for (int q = 0; q < SPB / 2; ++q) {
+          const float2 v = *reinterpret_cast<const float2*>(&sb[kk][tx + 16 * j][2 * q]);
+          b[j][2 * q] = v.x;
+          b[j][2 * q + 1] = v.y;
+        }
+#pragma unroll
+      for (int i = 0; i < MI; ++i)
+#pragma unroll
+        for (int j = 0; j < NJ; ++j)
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int t = 0; t < S - s; ++t) {  // level s + t (0-based), s + t <= S - 1
+              float& re = acc[i][j][s + t][0];
+              float& im = acc[i][j][s + t][1];
+              if constexpr (AC && BC) {
+                re = fmaf(a[i][2 * s], b[j][2 * t], re);
+                re = fmaf(-a[i][2 * s + 1], b[j][2 * t + 1], re);
+                im = fmaf(a[i][2 * s], b[j][2 * t + 1], im);
+                im = fmaf(a[i][2 * s + 1], b[j][2 * t], im);
+              } else if constexpr (AC) {
+                re = fmaf(a[i][2 * s], b[j][t], re);
+                im = fmaf(a[i][2 * s + 1], b[j][t], im);
+              } else if constexpr (BC) {
+                re = fmaf(a[i][s], b[j][2 * t], re);
+                im = fmaf(a[i][s], b[j][2 * t + 1], im);
+              } else {
+                re = fmaf(a[i][s], b[j][t], re);
+              }
+            }
+    }
+    __syncthreads();
+  }
+  // recombine the levels in int64 (0-based level l weighs 2^(-7(l + 2))) and store
+  const int u = 7 * ((S < 5 ? S : 5) + 1);
+#pragma unroll
+  for (int i = 0; i < MI; ++i)
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      const int r = ty + 16 * i, c = tx + 16 * j;
+      if (m0 + r >= g.M || n0 + c >= g.N) continue;
+      long long X[2] = {0, 0};
+#pragma unroll
+      for (int L = 0; L < S; ++L) {
+        const int sh = u - 7 * (L + 2);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          const long long v = (long long)__float2int_rn(acc[i][j][L][p]);
+          X[p] += sh >= 0 ? (v << sh) : (v >> (-sh));
+        }
+      }
+      const int E = ea[r] + eb[c] - u + (alpha_pow2 ? alpha_e : 0);
+      double vr, vi;
+      if (alpha_pow2) {
+        vr = scaled_i64_to_double(alpha_neg ? -X[0] : X[0], E);
+        vi = scaled_i64_to_double(alpha_neg ? -X[1] : X[1], E);
+      } else {
+        const double dr = scaled_i64_to_double(X[0], E), di = scaled_i64_to_double(X[1], E);
+        vr = g.ar * dr - g.ai * di;
+        vi = g.ar * di + g.ai * dr;
+      }
+      const long long off = coffm[r] + coffn[c];
+      if constexpr (CC) {
+        double2* C = static_cast<double2*>(g.C) + (size_t)zb * g.bsC;
+        if (g.acc) {
+          double2 cv = C[off];
+          cv.x += vr;
+          cv.y += vi;
+          C[off] = cv;
+        } else {
+          C[off] = make_double2(vr, vi);
+        }
+      } else {
+        double* C = static_cast<double*>(g.C) + (size_t)zb * g.bsC;
+        C[off] = g.acc ? C[off] + vr : vr;
+      }
+    }
+}
+
+template <bool AC, bool BC, bool CC, int S>
+static void launch_simt_tile(int tile, const GemmArgs& g, int nb, int p2, int e2, int n2, cudaStream_t st) {
+  const int bm = tile == 1 ? 16 : tile == 2 ? 64 : 32, bn = tile == 1 ? 64 : tile == 2 ? 16 : 32;
+  dim3 grid((unsigned)((g.N + bn - 1) / bn), (unsigned)((g.M + bm - 1) / bm), (unsigned)nb);
+  if (tile == 1)
+    simt_slices_kernel<AC, BC, CC, S, 16, 64><<<grid, 256, 0, st>>>(g, p2, e2, n2);
+  else if (tile == 2)
+    simt_slices_kernel<AC, BC, CC, S, 64, 16><<<grid, 256, 0, st>>>(g, p2, e2, n2);
+  else
+    simt_slices_kernel<AC, BC, CC, S, 32, 32><<<grid, 256, 0, st>>>(g, p2, e2, n2);
+}
+
+template <bool AC, bool BC, bool CC>
+static void launch_simt_typed(int tile, const GemmArgs& g, int nb, int S, int p2, int e2, int n2, cudaStream_t st) {
+  if (S == 6)
+    launch_simt_tile<AC, BC, CC, 6>(tile, g, nb, p2, e2, n2, st);
+  else
+    launch_simt_tile<AC, BC, CC, 5>(tile, g, nb, p2, e2, n2, st);
+}
+
+bool simt_slices_supported(int K, int S) { return K >= 1 && K <= kSimtMaxK && (S == 5 || S == 6); }
+
+cudaError_t launch_simt_slices(const Op& op, const void* A, const void* B, void* C, cudaStream_t st) {
+  GemmArgs g = op.g;
+  g.A = A;
+  g.B = B;
+  g.C = C;
+  const TcArgs& t = op.tc;
+  if (!simt_slices_supported(g.K, t.S) || g.atomic) return cudaErrorInvalidValue;
+  const int nb = g.nb < 1 ? 1 : g.nb;
+  // the tile with the least padding: 32 x 32, 16 x 64, 64 x 16
+  const long long M = g.M, N = g.N;
+  const long long pad[3] = {((M + 31) / 32 * 32) * ((N + 31) / 32 * 32), ((M + 15) / 16 * 16) * ((N + 63) / 64 * 64),
+                            ((M + 63) / 64 * 64) * ((N + 15) / 16 * 16)};
+  int tile = 0;
+  for (int q = 1; q < 3; ++q)
+    if (pad[q] < pad[tile]) tile = q;
+  const int bm = tile == 1 ? 16 : tile == 2 ? 64 : 32;
+  if ((M + bm - 1) / bm > 65535 || nb > 65535) return cudaErrorInvalidConfiguration;
+  const bool ac = op.dta == C64, bc = op.dtb == C64, cc = op.dtc == C64;
+  if (!cc && (ac || bc)) return cudaErrorInvalidValue;
+  if (ac && bc)
+    launch_simt_typed<true, true, true>(tile, g, nb, t.S, t.alpha_pow2, t.alpha_e, t.alpha_neg, st);
+  else if (ac)
+    launch_simt_typed<true, false, true>(tile, g, nb, t.S, t.alpha_pow2, t.alpha_e, t.alpha_neg, st);
+  else if (bc)
+    launch_simt_typed<false, true, true>(tile, g, nb, t.S, t.alpha_pow2, t.alpha_e, t.alpha_neg, st);
+  else if (cc)
+    launch_simt_typed<false, false, true>(tile, g, nb, t.S, t.alpha_pow2, t.alpha_e, t.alpha_neg, st);
+  else
+    launch_simt_typed<false, false, false>(tile, g, nb, t.S, t.alpha_pow2, t.alpha_e, t.alpha_neg, st);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 bool tc_available() { return true; }

@@ -712,8 +712,10 @@ bool Program::in_phase(const Op& op, Phase ph) {
 cudaError_t Program::launch_op(const Op& op, const std::vector<void*>& bases, cudaStream_t st) const {
   cudaError_t e = cudaSuccess;
   if (op.kind == OP_GEMM) {
-    e = launch_gemm(op, at(bases, op.sa, op.oa, op.dta), at(bases, op.sb, op.ob, op.dtb),
-                    const_cast<void*>(at(bases, op.sc, op.oc, op.dtc)), st);
+    const void* a = at(bases, op.sa, op.oa, op.dta);
+    const void* b = at(bases, op.sb, op.ob, op.dtb);
+    void* c = const_cast<void*>(at(bases, op.sc, op.oc, op.dtc));
+    e = op.backend == GB_SIMT ? launch_simt_slices(op, a, b, c, st) : launch_gemm(op, a, b, c, st);
   } else if (op.kind == OP_ADD) {
     AddArgs a = op.a;
     a.C = const_cast<void*>(at(bases, op.add_sc, op.add_oc, a.cc ? C64 : R64));
@@ -873,7 +875,8 @@ cudaError_t Program::run_dag(const std::vector<void*>& bases, cudaStream_t st, P
 
 static long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
 
-void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k, int min_mn) {
+void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k, int min_mn, int simt_max_k,
+                             long long simt_min_macs) {
   if (prec_mode != 1) return;
   if (S < 1 || S > 6) throw std::runtime_error("slices must be 1..6");
   constexpr int BM = 128, BN = 64, BK = 64;  // tensor-core tile (gemm_tc.h)
@@ -909,7 +912,27 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     }
     const long long M = op.g.M, N = op.g.N, K = op.g.K;
     if (M * N * K * std::max(op.g.nb, 1) < min_macs || K < min_k || std::min(M, N) < min_mn) {
-      push_op(op);
+      // short contractions: slice products on the FP32 pipe (the FP64 pipe
+      // is the one the elementwise ops and the update need)
+      const bool types_ok = op.dtc == C64 || (op.dta != C64 && op.dtb != C64);
+      if (K <= simt_max_k && simt_slices_supported((int)K, S) && types_ok &&
+          M * N * K * std::max(op.g.nb, 1) >= simt_min_macs) {
+        Op o = op;
+        o.backend = GB_SIMT;
+        o.g.nsplit = 1;
+        o.g.kchunk = (int)K;
+        o.g.atomic = 0;
+        o.tc = TcArgs{};
+        o.tc.S = S;
+        int e2 = 0;
+        const double fr = std::frexp(std::fabs(op.g.ar), &e2);
+        o.tc.alpha_pow2 = (op.g.ai == 0.0 && op.g.ar != 0.0 && fr == 0.5) ? 1 : 0;
+        o.tc.alpha_e = e2 - 1;
+        o.tc.alpha_neg = op.g.ar < 0.0 ? 1 : 0;
+        push_op(o);
+      } else {
+        push_op(op);
+      }
       continue;
     }
     if (err_slot < 0) {

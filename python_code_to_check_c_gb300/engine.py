@@ -144,6 +144,11 @@ class CCEngine:
         check(self.lib.tdcc_set_tc_policy(self.handle, int(min_macs), int(min_k), int(min_mn)),
               "tdcc_set_tc_policy")
 
+    def set_simt_policy(self, max_k: int = 64, min_macs: int = 1 << 14):
+        """Mixed mode: contractions left out by the tensor cores with K <= max_k
+        run as slice products on the FP32 pipe (max_k = 0: FP64)."""
+        check(self.lib.tdcc_set_simt_policy(self.handle, int(max_k), int(min_macs)), "tdcc_set_simt_policy")
+
     def set_memory_sharing(self, min_bytes: int = -1):
         """Workspace buffer sharing above min_bytes per program (-1: default
         1 GiB, 0: always)."""

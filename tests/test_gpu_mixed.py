@@ -112,3 +112,53 @@ def test_mixed_trajectory_o10_v14(method):
         eng.close()
     err = np.abs(_np(mumx) - _np(mu64)).max()
     assert err < MU_TOL, err
+
+
+@pytest.mark.parametrize("fn,name,args", [("T2eq_rhs", "T2", "t"), ("lam_1eq_rhs", "L1", "l"),
+                                          ("lam2eq_rhs", "L2", "l"), ("L1eq_rhs_CC2", "L1_CC2", "l")])
+def test_short_contractions_on_the_fp32_pipe(fn, name, args):
+    """Slice products on the FP32 pipe (tensor cores off, every contraction
+    with K <= 64 on the SIMT path): the residuals meet the same bar, the
+    error shrinks with more slices, and the path is really taken."""
+    from python_code_to_check_c_gb300.engine import CCEngine, profile_step
+    from python_code_to_check_c_gb300._lib import make_field
+    d, sysm = load("golden_o6_v10.npz")
+    eng = CCEngine.from_system(sysm)
+    try:
+        eng.set_tc_policy(1 << 62, 1 << 30, 1)  # nothing on the tensor cores
+        eng.set_simt_policy(64, 0)
+        a = (d["t1"], d["t2"]) if args == "t" else (d["t1"], d["t2"], d["l1"], d["l2"])
+        errs = []
+        for S in (5, 6):  # the FP32-pipe path takes 5 or 6 slices
+            eng.set_precision("mixed", S)
+            got = _np(getattr(eng, fn)(*a, d["F"]))
+            errs.append(rel_err(got, d[name]))
+        assert errs[0] < RES_TOL, errs
+        assert errs[0] > errs[1], errs
+        st = [d["t1"] + 0j, d["t2"] + 0j, d["l1"] + 0j, d["l2"] + 0j]
+        recs = profile_step(eng, "CCSD", st, 0.0, 0.01, make_field("sin", 0.002, 0.923))
+        assert sum(1 for r in recs if r["kind"] == 0 and r["backend"] == 2) >= 10
+    finally:
+        eng.close()
+
+
+def test_simt_path_keeps_trajectories():
+    """Default routing (tensor cores for the large contractions, the FP32
+    pipe for the short ones) against the same without the FP32-pipe path."""
+    from python_code_to_check_c_gb300._lib import make_field
+    from python_code_to_check_c_gb300.engine import CCEngine
+    d, sysm = load("golden_o6_v10.npz")
+    st = [d["t1"] + 0j, d["t2"] + 0j, d["l1"] + 0j, d["l2"] + 0j]
+    out = []
+    for max_k in (64, 0):
+        eng = CCEngine.from_system(sysm)
+        try:
+            eng.set_precision("mixed", 5)
+            eng.set_tc_policy(1 << 16, 32, 1)
+            eng.set_simt_policy(max_k, 0)
+            _, traj = eng.propagate("CCSD", st, 0.0, 0.01, 20, make_field("sin", 0.005, 0.923))
+            eng.check_errors()
+            out.append(_np(traj))
+        finally:
+            eng.close()
+    assert np.abs(out[0] - out[1]).max() < MU_TOL
