@@ -45,11 +45,11 @@ AMPS = (0.001, 0.002, 0.005, 0.01)
 W0S = (0.5, 0.923)
 POLS = (0, 1, 2)
 REF_TRAJ = (2, 0.002, 0.923)  # the single-trajectory configuration (z, A, w0)
-# DRAM bytes (read + write) per launch of the step's dominant slice products, from one
-# single-pass ncu capture (dram__bytes_read.sum, dram__bytes_write.sum) of the T2 program at
-# 24 trajectories: the ladder with the shared integral operand, and the batched Wmnij product
-TRAFFIC_PER_LAUNCH = {("ccsd_t2:abef,ijef->ijab", 24): 150.44e6 + 36.12e6,
-                      ("ccsd_t2:mnij,mnab->ijab", 24): 154.17e6 + 28.77e6}
+# DRAM bytes (read + write) per launch of the slice-product kernel, averaged over the 187
+# launches of one 24-trajectory step: a single-pass ncu capture (dram__bytes_read.sum,
+# dram__bytes_write.sum, -k regex:ozaki) of `profile_case --step --precision mixed --nb 24`
+TRAFFIC_PER_LAUNCH = {("ozaki_kernel", 24): (22811.92e6 + 2370.70e6) / 187}
+TRAFFIC_SOURCE = "ncu capture of all slice-product launches of one 24-trajectory step (mean per launch)"
 
 
 def parse():
@@ -396,31 +396,42 @@ def run_ours(args, rank, world, local_rank):
         return
 
     # ---- roofline of the dominant kernel (CUDA events per launch) ----
+    # launches are grouped by kernel: the slice products (tensor cores), the
+    # FP32-pipe slice products, FP64 contractions, operand packing and the
+    # elementwise ops; the roofline line describes the kernel with the most time
     recs = profile_step(eng, args.method, bstate, 0.0, DT, fields[0])
-    by = {}
+
+    def kernel_of(r):
+        if r["kind"] == 0:
+            return {1: "ozaki_kernel", 2: "simt_slices_kernel"}.get(r["backend"], "gemm_f64_kernel")
+        if r["tag"].endswith(":packA") or r["tag"].endswith(":packB"):
+            return "pack_kernel"
+        return "add_kernel" if r["kind"] == 1 else "rk4/trace kernels"
+
+    by, by_tag = {}, {}
     for r in recs:
-        k = (r["tag"], r["backend"])
-        a = by.setdefault(k, {"ms": 0.0, "n": 0, "flops": 0.0, "bytes": 0.0, "kind": r["kind"]})
-        a["ms"] += r["ms"]
-        a["n"] += 1
-        a["flops"] += r["flops"]
-        a["bytes"] += r["bytes"]
+        for d, k in ((by, kernel_of(r)), (by_tag, (r["tag"], r["backend"]))):
+            a = d.setdefault(k, {"ms": 0.0, "n": 0, "flops": 0.0, "bytes": 0.0})
+            a["ms"] += r["ms"]
+            a["n"] += 1
+            a["flops"] += r["flops"]
+            a["bytes"] += r["bytes"]
     tot = sum(a["ms"] for a in by.values())
-    (tag, backend), dom = max(by.items(), key=lambda kv: kv[1]["ms"])
+    kern, dom = max(by.items(), key=lambda kv: kv[1]["ms"])
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     pairs = 15  # slice products per FP64 product with 5 slices (levels 2..6)
-    if dom["kind"] == 0 and backend == 1:
+    if kern == "ozaki_kernel":
         achieved = dom["flops"] / (dom["ms"] / 1e3) / 1e12
         peak = peaks.get("bf16_tflops", 1900.0)
         roof = {"bound": "tensor", "unit": "TFLOP/s",
                 "peak_source": "measured bf16 burst (MEASURED_PEAKS.json)" if "bf16_tflops" in peaks else "fallback",
-                "achieved_is": "FP64-equivalent algorithmic flops of the contraction / launch time",
+                "achieved_is": "FP64-equivalent algorithmic flops of the step's slice products / their launch time",
                 "tensor_work_frac": achieved * pairs / peak}
-    elif dom["kind"] == 0:
+    elif kern in ("gemm_f64_kernel", "simt_slices_kernel"):
         achieved = dom["flops"] / (dom["ms"] / 1e3) / 1e12
         peak = 1.25
         roof = {"bound": "fp64", "unit": "TFLOP/s", "peak_source": "nominal GB300 FP64 (no measured FP64 peak)"}
@@ -428,14 +439,17 @@ def run_ours(args, rank, world, local_rank):
         achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "hbm", "unit": "GB/s", "peak_source": "measured HBM copy (MEASURED_PEAKS.json)"}
-    traffic = TRAFFIC_PER_LAUNCH.get((tag, nb))
-    roof.update({"kernel": tag, "achieved": achieved, "peak": peak, "frac": achieved / peak,
+    traffic = TRAFFIC_PER_LAUNCH.get((kern, nb))
+    roof.update({"kernel": kern, "achieved": achieved, "peak": peak, "frac": achieved / peak,
                  "traffic": traffic,
-                 "traffic_source": "ncu capture of the same contraction at 24 trajectories" if traffic else None,
+                 "traffic_source": TRAFFIC_SOURCE if traffic else None,
+                 "algorithmic_bytes_per_launch": dom["bytes"] / dom["n"],
                  "launches_per_step": dom["n"], "share_of_step": dom["ms"] / tot,
                  "avg_launch_ms": dom["ms"] / dom["n"]})
-    top = sorted(by.items(), key=lambda kv: -kv[1]["ms"])[:6]
-    breakdown = [{"kernel": k[0], "tc": k[1], "share": a["ms"] / tot, "launches": a["n"]} for k, a in top]
+    breakdown = [{"kernel": k, "share": a["ms"] / tot, "launches": a["n"]}
+                 for k, a in sorted(by.items(), key=lambda kv: -kv[1]["ms"])]
+    top = sorted(by_tag.items(), key=lambda kv: -kv[1]["ms"])[:6]
+    top_contractions = [{"op": k[0], "backend": k[1], "share": a["ms"] / tot, "launches": a["n"]} for k, a in top]
 
     adj = None
     if args.adjoint_steps > 0:
@@ -469,7 +483,8 @@ def run_ours(args, rank, world, local_rank):
                    "l2": f"per-step working set {ws / 2**30:.1f} GiB workspace + "
                          f"{sysm.n ** 4 * 8 / 2**20:.0f} MiB integrals (> 129 MB L2), no flush",
                    "ground_state": gs_info},
-        "roofline": roof, "kernel_breakdown": breakdown, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roof, "kernel_breakdown": breakdown, "top_contractions": top_contractions,
+        "cpu_baseline": cpu, "e2e": e2e,
         "fp64_form": fp64, "single_trajectory_mixed": single_mixed, "adjoint": adj,
         "gpu_launches": launches, "launches_per_step": launches / args.steps, "clocks": clk.summary(),
         "finite": finite,
