@@ -594,8 +594,10 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
       const int m0w = AC ? ((mt * TC_BM + q * 32) >> 1) : (mt * TC_BM + q * 32);
       constexpr int NCW = ncol_log / kWq;  // logical columns of this warp (<= 32)
       // every lane owns a (row, column) pair: NCW columns by 32 / NCW rows per
-      // pass; the loads of up to four passes (accumulated outputs) are in
-      // flight together
+      // pass.  Accumulated outputs are added in L2 (reductions without a
+      // return value), so the pass issues no load: one writer per element
+      // and launch (split K aside), so the single addition c + v is the same
+      // as a read-modify-write.
       static_assert(32 % NCW == 0, "columns per warp divide the warp");
       constexpr int RPP = 32 / NCW;
       constexpr int NPASS = (rows_out + RPP - 1) / RPP;
@@ -603,41 +605,27 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
       const int cc = hcol * NCW + lc;  // this lane's column while storing
       const long long cn = sh->col_off[cc];
       const int nrows = min(rows_out, g.M - m0w);
-#pragma unroll
-      for (int p0 = 0; p0 < NPASS; p0 += 4) {
-        long long off[4];
-        double2 old[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int r = (p0 + i) * RPP + lrw;
-          // row offsets live in the lanes of the rows' TMEM rows
-          const long long cm = __shfl_sync(0xffffffffu, coffm, (AC ? 2 * r : r) & 31);
-          off[i] = (p0 + i < NPASS && r < nrows && cn >= 0) ? cm + cn : -1;
-          old[i] = make_double2(0.0, 0.0);
-        }
-        if (g.acc && !g.atomic) {
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (off[i] >= 0) old[i] = g.cc ? C[off[i]] : make_double2(Cr[off[i]], 0.0);
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          if (off[i] < 0) continue;
-          const int r = (p0 + i) * RPP + lrw;
-          const double2 v = stage[r * RS + cc];
-          if (g.cc) {
-            if (g.atomic) {
-              atomicAdd(&C[off[i]].x, v.x);
-              atomicAdd(&C[off[i]].y, v.y);
-            } else {
-              C[off[i]] = g.acc ? make_double2(old[i].x + v.x, old[i].y + v.y) : v;
-            }
+      const bool red = g.acc || g.atomic;
+#pragma unroll 4
+      for (int p = 0; p < NPASS; ++p) {
+        const int r = p * RPP + lrw;
+        // row offsets live in the lanes of the rows' TMEM rows
+        const long long cm = __shfl_sync(0xffffffffu, coffm, (AC ? 2 * r : r) & 31);
+        if (r >= nrows || cn < 0) continue;
+        const long long off = cm + cn;
+        const double2 v = stage[r * RS + cc];
+        if (g.cc) {
+          if (red) {
+            atomicAdd(&C[off].x, v.x);
+            atomicAdd(&C[off].y, v.y);
           } else {
-            if (g.atomic)
-              atomicAdd(&Cr[off[i]], v.x);
-            else
-              Cr[off[i]] = g.acc ? old[i].x + v.x : v.x;
+            C[off] = v;
           }
+        } else {
+          if (red)
+            atomicAdd(&Cr[off], v.x);
+          else
+            Cr[off] = v.x;
         }
       }
     }
