@@ -844,19 +844,21 @@ __global__ void __launch_bounds__(256, 2) simt_slices_kernel(const GemmArgs g, i
         vi = g.ar * di + g.ai * dr;
       }
       const long long off = coffm[r] + coffn[c];
+      // accumulation as an L2 reduction (one writer per element)
       if constexpr (CC) {
         double2* C = static_cast<double2*>(g.C) + (size_t)zb * g.bsC;
         if (g.acc) {
-          double2 cv = C[off];
-          cv.x += vr;
-          cv.y += vi;
-          C[off] = cv;
+          atomicAdd(&C[off].x, vr);
+          atomicAdd(&C[off].y, vi);
         } else {
           C[off] = make_double2(vr, vi);
         }
       } else {
         double* C = static_cast<double*>(g.C) + (size_t)zb * g.bsC;
-        C[off] = g.acc ? C[off] + vr : vr;
+        if (g.acc)
+          atomicAdd(&C[off], vr);
+        else
+          C[off] = vr;
       }
     }
 }

@@ -180,24 +180,17 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const GemmArgs g) {
       if constexpr (CC) {
         double2* C = static_cast<double2*>(g.C) + zb * g.bsC;
         const double2 v = make_double2(g.ar * s.x - g.ai * s.y, g.ar * s.y + g.ai * s.x);
-        if (g.atomic) {
+        if (g.atomic || g.acc) {  // L2 reductions (one writer per element unless split)
           atomicAdd(&C[off].x, v.x);
           atomicAdd(&C[off].y, v.y);
-        } else if (g.acc) {
-          double2 c = C[off];
-          c.x += v.x;
-          c.y += v.y;
-          C[off] = c;
         } else {
           C[off] = v;
         }
       } else {
         double* C = static_cast<double*>(g.C) + zb * g.bsC;
         const double v = g.ar * s.x;
-        if (g.atomic)
+        if (g.atomic || g.acc)
           atomicAdd(&C[off], v);
-        else if (g.acc)
-          C[off] += v;
         else
           C[off] = v;
       }
@@ -315,19 +308,23 @@ __global__ void __launch_bounds__(256) add_kernel(const AddArgs a) {
 #pragma unroll
     for (int q = 0; q < kAddDims; ++q)
       if (q < a.nd) oc += (long long)ii[q] * a.sC[q];
+    // accumulation as an L2 reduction (no return value): one writer per
+    // element, so the single addition c + s equals a read-modify-write, and
+    // neither the load nor the add occupies the SM (its FP64 pipe is narrow)
     if (a.cc) {
       double2* C = static_cast<double2*>(a.C);
       if (a.acc) {
-        double2 c = C[oc];
-        c.x += s.x;
-        c.y += s.y;
-        C[oc] = c;
+        atomicAdd(&C[oc].x, s.x);
+        atomicAdd(&C[oc].y, s.y);
       } else {
         C[oc] = s;
       }
     } else {
       double* C = static_cast<double*>(a.C);
-      C[oc] = a.acc ? C[oc] + s.x : s.x;
+      if (a.acc)
+        atomicAdd(&C[oc], s.x);
+      else
+        C[oc] = s.x;
     }
   }
 }
