@@ -301,8 +301,13 @@ __global__ void __launch_bounds__(256) add_kernel(const AddArgs a) {
         const double2 y = ld(T.B, ob, T.bc);
         x = make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
       }
-      s.x += T.cr * x.x - T.ci * x.y;
-      s.y += T.cr * x.y + T.ci * x.x;
+      if (T.ci == 0.0) {  // real coefficients (almost all): half the FP64 operations
+        s.x = fma(T.cr, x.x, s.x);
+        s.y = fma(T.cr, x.y, s.y);
+      } else {
+        s.x += T.cr * x.x - T.ci * x.y;
+        s.y += T.cr * x.y + T.ci * x.x;
+      }
     }
     long long oc = 0;
 #pragma unroll
