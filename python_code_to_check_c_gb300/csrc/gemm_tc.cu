@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
     }
     for (int part = 0; part < per; ++part) {
       const unsigned long long f = fixed_point(x[part], e, nbits);
-      const bool neg = x[part] < 0.0;
+      const bool neg = __double_as_longlong(x[part]) < 0;  // sign bit: no FP64 compare
       const size_t base = (prow + part) * p.K_pad + k;
       for (int s = 0; s < p.S; ++s) {
         const int q = (int)((f >> (7 * (p.S - 1 - s))) & 127ull);
@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(256, 2) simt_slices_kernel(const GemmArgs g, i
       float* dst = isA ? &sa[kk][r][0] : &sb[kk][r][0];
       for (int part = 0; part < per; ++part) {
         const unsigned long long f = fixed_point(x[part], e, nbits);
-        const bool neg = x[part] < 0.0;
+        const bool neg = __double_as_longlong(x[part]) < 0;  // sign bit: no FP64 compare
 #pragma unroll
         for (int s = 0; s < S; ++s) {
           const int q = (int)((f >> (7 * (S - 1 - s))) & 127ull);
