@@ -32,3 +32,19 @@ def test_tei_from_df_matches_host_provider():
     # <pq||rs> = -<pq||sr> = -<qp||rs>
     assert np.abs(g + g.transpose(0, 1, 3, 2)).max() == 0.0
     assert np.abs(g + g.transpose(1, 0, 2, 3)).max() <= 1e-15 * np.abs(g).max()
+
+
+def test_trajectory_table_round_trip(tmp_path):
+    """The spectrum reads the propagation's H2O.csv (index, time, mu_real,
+    mu_imag) as the table writer produces it, values exactly."""
+    from python_code_to_check_c_gb300 import restart_io
+    from python_code_to_check_c_gb300.spectrum import read_trajectory
+    rng = np.random.default_rng(3)
+    t = np.arange(1, 11) * 0.005
+    mu = rng.standard_normal(10) + 1j * rng.standard_normal(10)
+    path = str(tmp_path / "H2O.csv")
+    restart_io.write_table(path, ("time", "mu_real", "mu_imag"), [(a, b.real, b.imag) for a, b in zip(t, mu)], 0,
+                           False)
+    t2, mu2 = read_trajectory(path)
+    np.testing.assert_array_equal(t2, t)
+    np.testing.assert_array_equal(mu2, mu)
