@@ -50,3 +50,22 @@ def test_version_and_error_path(lib):
     assert "o and v" in _lib.last_error()
     rc = lib.tdcc_rhs(None, 0, 0, None, None, None, None, None, None, None)
     assert rc == -1
+
+
+def test_argument_checks_without_a_gpu(lib):
+    """Bad arguments fail with TDCC_ERR_ARG and a message before any CUDA
+    call: the policy setters, reverse-mode storage, integral build, spectrum."""
+    from python_code_to_check_c_gb300 import _lib
+    assert lib.tdcc_set_tc_policy(None, 0, 1, 1) == -1
+    assert lib.tdcc_set_simt_policy(None, 64, 0) == -1
+    assert lib.tdcc_set_adjoint_store(None, 1) == -1
+    assert lib.tdcc_set_memory_sharing(None, 0) == -1
+    assert lib.tdcc_tei_from_df(None, 4, 8, None, None) == -1
+    assert "NULL" in _lib.last_error()
+    dummy = ctypes.c_void_p(16)
+    assert lib.tdcc_tei_from_df(dummy, 0, 8, dummy, None) == -1
+    assert "sizes" in _lib.last_error()
+    assert lib.tdcc_spectrum(None, 8, 1, 0.1, None, None, None, None) == -1
+    assert lib.tdcc_spectrum(dummy, 0, 1, 0.1, dummy, dummy, None, None) == -1
+    assert lib.tdcc_spectrum(dummy, 8, 1, 0.0, dummy, dummy, None, None) == -1
+    assert "dt" in _lib.last_error()
