@@ -266,6 +266,24 @@ def adjoint_cost(sysm, method, gs, nsteps):
             "dJ_dA": gA, "dJ_dA_central_difference": fd, "rel_err": abs(gA - fd) / max(abs(fd), 1e-300)}
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest value over the ranks (the slowest replica's time); the
+    tensor lives on `device` (CUDA under NCCL, CPU under gloo)."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, trajectories: int, steps: int, ms: float) -> float:
+    """Trajectory-steps per second of all replicas together: every rank
+    advances `trajectories` trajectories by `steps` steps; `ms` is the
+    slowest rank's time."""
+    return world * trajectories * steps / (ms / 1e3)
+
+
 def timed(fn):
     import torch
     torch.cuda.synchronize()
@@ -328,13 +346,8 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
     barrier()
     launches = launch_count() - n0
-    ms = e0.elapsed_time(e1)
-    t_max = ms
-    if world > 1:
-        tt = torch.tensor([ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * nb * args.steps / (t_max / 1e3)
+    t_max = max_over_ranks(e0.elapsed_time(e1), world, dev)
+    value = whole_job_rate(world, nb, args.steps, t_max)
     finite = bool(torch.isfinite(torch.view_as_real(traj)).all().item())
     eng.check_errors()
 
@@ -383,12 +396,8 @@ def run_ours(args, rank, world, local_rank):
         t_e2e += DT
     f1.record()
     torch.cuda.synchronize()
-    e2e_ms = f0.elapsed_time(f1)
-    if world > 1:
-        tt = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
-    e2e = {"value": world * nb * ke / (e2e_ms / 1e3), "unit": "steps/s", "h2d_bytes_per_step": h2d,
+    e2e_ms = max_over_ranks(f0.elapsed_time(f1), world, dev)
+    e2e = {"value": whole_job_rate(world, nb, ke, e2e_ms), "unit": "steps/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "steps": ke, "trajectories": nb}
 
     if rank != 0:
