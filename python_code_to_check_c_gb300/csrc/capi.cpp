@@ -264,7 +264,13 @@ ProgInst& get_density(tdcc_system s) {
 }
 
 void build_program(Program& p, int method, int block, int n_mu, int nb);
-void plan_activations(ProgInst& ai, const Program& fwd);
+struct ActPlan {
+  std::vector<int> slot;          // forward slots kept
+  std::vector<char> stage;        // 1: one value per stage, 0: one per step
+  std::vector<long long> off8;    // offset (8-byte words) in the step's prologue or stage part
+  long long pro8 = 0, stage8 = 0; // words of the prologue part and of one stage part
+};
+ActPlan plan_activations(const Program& adj, size_t nfwd, const Program& fwd);
 void reset_programs(tdcc_system s);
 
 // Reverse-mode program of (method, block); block 4 = density.  Its slots
@@ -293,7 +299,14 @@ ProgInst& get_adj(tdcc_system s, int method, int block) {
   s->ws_bytes += pi->bytes;
   pi->setup_done = true;  // no integral-only ops in a reverse-mode program
   pi->dag.init(pi->prog->ops.size(), 4);
-  if (block < 4) plan_activations(*pi, *get_rhs(s, method, block).prog);
+  if (block < 4) {
+    const ActPlan ap = plan_activations(*pi->prog, pi->nfwd, *get_rhs(s, method, block).prog);
+    pi->act_slot = ap.slot;
+    pi->act_stage = ap.stage;
+    pi->act_off8 = ap.off8;
+    pi->act_pro8 = ap.pro8;
+    pi->act_stage8 = ap.stage8;
+  }
   slot = std::move(pi);
   return *slot;
 }
@@ -303,34 +316,33 @@ ProgInst& get_adj(tdcc_system s, int method, int block) {
 // integral-only setup.  A slot written by a stage op holds one value per
 // stage; the others one per step.  Binding the reverse-mode program to the
 // record gives it the values the forward step computed, so it need not run
-// the forward ops again.
-void plan_activations(ProgInst& ai, const Program& fwd) {
-  std::vector<char> rd(ai.nfwd, 0), pro(ai.nfwd, 0), stg(ai.nfwd, 0);
-  for (const Op& op : ai.prog->ops)
+// the forward ops again.  `nfwd`: the forward slots (the reverse-mode
+// program's first slots).
+ActPlan plan_activations(const Program& adj, size_t nfwd, const Program& fwd) {
+  std::vector<char> rd(nfwd, 0), pro(nfwd, 0), stg(nfwd, 0);
+  for (const Op& op : adj.ops)
     for (int r : op.reads)
-      if (r >= 0 && r < (int)ai.nfwd) rd[r] = 1;
+      if (r >= 0 && r < (int)nfwd) rd[r] = 1;
   for (const Op& op : fwd.ops) {
-    if (op.write < 0 || op.write >= (int)ai.nfwd) continue;
+    if (op.write < 0 || op.write >= (int)nfwd) continue;
     if (Program::in_phase(op, Program::STAGE))
       stg[op.write] = 1;
     else if (Program::in_phase(op, Program::PROLOGUE))
       pro[op.write] = 1;
   }
-  ai.act_slot.clear();
-  ai.act_stage.clear();
-  ai.act_off8.clear();
-  ai.act_pro8 = ai.act_stage8 = 0;
+  ActPlan ap;
   for (int pass = 0; pass < 2; ++pass)
-    for (size_t i = 0; i < ai.nfwd; ++i) {
+    for (size_t i = 0; i < nfwd; ++i) {
       if (!rd[i] || !(pro[i] || stg[i]) || (pass == 1) != (stg[i] != 0)) continue;
       const SlotInfo& si = fwd.slots[i];
       const long long w = (si.numel * elem_bytes(si.dt) + 7) / 8;
-      long long& acc = pass ? ai.act_stage8 : ai.act_pro8;
-      ai.act_slot.push_back((int)i);
-      ai.act_stage.push_back((char)pass);
-      ai.act_off8.push_back(acc);
+      long long& acc = pass ? ap.stage8 : ap.pro8;
+      ap.slot.push_back((int)i);
+      ap.stage.push_back((char)pass);
+      ap.off8.push_back(acc);
       acc += (w + 31) / 32 * 32;  // 256-byte aligned entries
     }
+  return ap;
 }
 
 // copies of one phase's activations (stage 0: prologue) into the step store
@@ -1727,8 +1739,10 @@ std::string program_json(const Program& p) {
   for (size_t i = 0; i < p.ops.size(); ++i) {
     const Op& op = p.ops[i];
     j += i ? "," : "";
-    const std::string var =
-        std::string(op.varying ? "true" : "false") + ",\"const\":" + (op.is_const ? "true" : "false");
+    // phase flags, then the slots the op reads and writes (dependency analysis)
+    const std::string var = std::string(op.varying ? "true" : "false") + ",\"const\":" +
+                            (op.is_const ? "true" : "false") + ",\"reads\":" +
+                            jarr(op.reads.data(), (int)op.reads.size()) + ",\"write\":" + std::to_string(op.write);
     if (op.kind == OP_GEMM) {
       const GemmArgs& g = op.g;
       j += "{\"kind\":\"gemm\",\"tag\":\"" + op.tag + "\",\"varying\":" + var +
@@ -1791,7 +1805,15 @@ extern "C" long long tdcc_adjoint_program_json(int o, int v, int method, int blo
     build_adjoint(p, a, adj_of);
     std::string j = program_json(a);
     j.pop_back();  // '}'
-    j += ",\"nfwd\":" + std::to_string(p.slots.size()) + ",\"adj_of\":" + jarr(adj_of.data(), (int)adj_of.size()) + "}";
+    j += ",\"nfwd\":" + std::to_string(p.slots.size()) + ",\"adj_of\":" + jarr(adj_of.data(), (int)adj_of.size());
+    if (block < 4) {  // the activation record the step graph keeps for this program
+      const ActPlan ap = plan_activations(a, p.slots.size(), p);
+      std::vector<int> st(ap.stage.begin(), ap.stage.end());
+      j += ",\"act\":{\"pro8\":" + std::to_string(ap.pro8) + ",\"stage8\":" + std::to_string(ap.stage8) +
+           ",\"slots\":" + jarr(ap.slot.data(), (int)ap.slot.size()) + ",\"stage\":" +
+           jarr(st.data(), (int)st.size()) + ",\"off8\":" + jarr(ap.off8.data(), (int)ap.off8.size()) + "}";
+    }
+    j += "}";
     if (!buf || len < j.size() + 1) return fail(TDCC_ERR_LIMIT, "buffer too small: need " + std::to_string(j.size() + 1));
     memcpy(buf, j.c_str(), j.size() + 1);
     return (long long)j.size();
