@@ -4,7 +4,8 @@
 // Operand packing (pack_kernel): each row of A (an M x K view) and each
 // column of B (a K x N view) is scaled by 2^-e with e the binary exponent of
 // its largest magnitude, then cut into S slices of 7 bits,
-//     x * 2^-e = sum_s q_s 2^(-7s),  q_s integers, |q_1| <= 128, |q_s| <= 64,
+//     x * 2^-e = sum_s q_s 2^(-7s),  q_s integers, |q_1| <= 128, |q_s| <= 64
+// (balanced digits: each lower digit in [-64, 63], carries into the next),
 // each exactly representable in BF16.  Complex operands contribute two packed
 // rows (real, imaginary) per logical row.  Packed layout: [S][rows][K] BF16,
 // K contiguous (K-major for UMMA), rows and K zero-padded to the tile sizes.
@@ -84,11 +85,32 @@ __device__ __forceinline__ unsigned long long fixed_point(double x, int e, int n
   return M >> (-sh);
 }
 
+// The digits of f < 2^(7S) in balanced form, least significant first:
+// every digit below the top one in [-64, 63] (a digit >= 64 becomes d - 128
+// with a carry into the next), the top one in [0, 128].  The value is f
+// itself, sum_s q[s] 2^(7(S-1-s)), and products of digits stay within 2^14.
+template <int SMAX>
+__device__ __forceinline__ void balanced_digits(unsigned long long f, int S, int (&q)[SMAX]) {
+#pragma unroll
+  for (int i = SMAX - 1; i >= 1; --i)
+    if (i < S) {
+      int d = (int)(f & 127ull);
+      f >>= 7;
+      if (d >= 64) {
+        d -= 128;
+        ++f;
+      }
+      q[i] = d;
+    }
+  q[0] = (int)f;
+}
+
 // One block per logical row (per batch; the real and imaginary rows of a
 // complex row together): pass 1 takes the binary exponent e of the row's
 // max |x| (max = f 2^e, f in [0.5, 1); integer ops on the bit patterns, the
 // order of |x| for finite doubles), pass 2 cuts |x| 2^-e truncated to 7S
-// bits into S signed 7-bit digits (|q_s| <= 127, exact in BF16):
+// bits into S balanced digits (|q_1| <= 128, |q_s| <= 64, exact in BF16) and
+// gives them the sign of x:
 //   x 2^-e ~= sum_s q_s 2^(-7s).
 // The real and imaginary rows share e, so that the slice-product epilogue
 // combines re*re - im*im and re*im + im*re exactly in integers.  K padding
@@ -149,10 +171,11 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
       const unsigned long long f = fixed_point(x[part], e, nbits);
       const bool neg = __double_as_longlong(x[part]) < 0;  // sign bit: no FP64 compare
       const size_t base = (prow + part) * p.K_pad + k;
-      for (int s = 0; s < p.S; ++s) {
-        const int q = (int)((f >> (7 * (p.S - 1 - s))) & 127ull);
-        out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -q : q));
-      }
+      int qd[TC_MAX_SLICES];
+      balanced_digits(f, p.S, qd);
+#pragma unroll
+      for (int s = 0; s < TC_MAX_SLICES; ++s)
+        if (s < p.S) out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -qd[s] : qd[s]));
     }
   }
 }
@@ -760,11 +783,10 @@ __global__ void __launch_bounds__(256, 2) simt_slices_kernel(const GemmArgs g, i
       for (int part = 0; part < per; ++part) {
         const unsigned long long f = fixed_point(x[part], e, nbits);
         const bool neg = __double_as_longlong(x[part]) < 0;  // sign bit: no FP64 compare
+        int qd[S];
+        balanced_digits(f, S, qd);
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-          const int q = (int)((f >> (7 * (S - 1 - s))) & 127ull);
-          dst[s * per + part] = (float)(neg ? -q : q);
-        }
+        for (int s = 0; s < S; ++s) dst[s * per + part] = (float)(neg ? -qd[s] : qd[s]);
       }
     }
     __syncthreads();
