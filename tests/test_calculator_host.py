@@ -138,3 +138,25 @@ def test_timeout_stop_and_restart(tmp_path):
     assert np.abs(out2["mu"] - mus[1:]).max() < 1e-14
     rows = (tmp_path / "H2O.csv").read_text().splitlines()
     assert len(rows) == 1 + 4 + 4 and rows[5].startswith("1,")
+
+
+def test_psi4_construction_path(tmp_path):
+    """CC_Calculator(psi4) as the reference's scripts call it: the system comes
+    from the psi4 integral adapter (here the psi4 stand-in), and the loop runs
+    on it."""
+    import fake_psi4
+    from python_code_to_check_c_gb300.system import system_from_psi4
+    psi4 = fake_psi4.make()
+    c = CC_Calculator(psi4, outdir=str(tmp_path), verbose=False, w0=0.923, A=0.002, t0=0.0, dt=0.01, precs=15)
+    ref = system_from_psi4(fake_psi4.make())
+    assert (c.system.o, c.system.v, c.ndocc) == (ref.o, ref.v, ref.o // 2)
+    np.testing.assert_array_equal(c.system.fock, ref.fock)
+    eng = OracleEngine(c.system, 0.002, 0.923)
+    c.engine = lambda F=None: eng
+    o, v = c.system.o, c.system.v
+    rng = np.random.default_rng(2)
+    st = (0.01 * rng.standard_normal((o, v)) + 0j, np.zeros((o, o, v, v)) + 0j,
+          0.01 * rng.standard_normal((o, v)) + 0j, np.zeros((o, o, v, v)) + 0j)
+    out = c.Runge_Kutta_solver(c.system.fock, *st, 0.923, 0.002, 0.0, 0.05, 0.01, None, 15)
+    _, mus, _ = eng.orc.propagate("CCSD", c.system.fock, list(st), 0.0, 0.01, 5, eng.Vt, 15)
+    assert out["steps"] == 5 and np.array_equal(out["mu"], mus[1:])
