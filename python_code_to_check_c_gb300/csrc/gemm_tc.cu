@@ -998,8 +998,11 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
 
 template <class C>
 static cudaError_t launch_variant(const TcArgs& a0, const void* packA, const void* packB, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
+  // kernel attributes, once per process (engines on several host threads
+  // may launch their first slice products together)
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
     cudaError_t e = cudaFuncSetAttribute(ozaki_kernel<true, true, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(ozaki_kernel<true, false, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
@@ -1020,9 +1023,9 @@ static cudaError_t launch_variant(const TcArgs& a0, const void* packA, const voi
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(ozaki_kernel<false, false, C>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+    attr_err = e;
+  });
+  if (attr_err != cudaSuccess) return attr_err;
   TcArgs a = a0;
   if (a.S > C::STAGES) return cudaErrorInvalidValue;  // the ring holds one K block's slices
   int cols = 32;
