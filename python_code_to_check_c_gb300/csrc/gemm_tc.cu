@@ -945,17 +945,18 @@ cudaError_t launch_simt_slices(const Op& op, const void* A, const void* B, void*
 // ---------------------------------------------------------------------------
 bool tc_available() { return true; }
 
+// the driver's tensor-map encoder, looked up once (thread-safe static init)
 static PFN_cuTensorMapEncodeTiled_v12000 encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
             cudaSuccess ||
         !p)
-      throw std::runtime_error("cuTensorMapEncodeTiled unavailable");
-    fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }();
+  if (!fn) throw std::runtime_error("cuTensorMapEncodeTiled unavailable");
   return fn;
 }
 
