@@ -47,7 +47,7 @@ POLS = (0, 1, 2)
 REF_TRAJ = (2, 0.002, 0.923)  # the single-trajectory configuration (z, A, w0)
 # DRAM bytes (read + write) per launch of the slice-product kernel, averaged over the 187
 # launches of one 24-trajectory step: a single-pass ncu capture (dram__bytes_read.sum,
-# dram__bytes_write.sum, -k regex:ozaki) of `profile_case --step --precision mixed --nb 24`
+# dram__bytes_write.sum, -k regex:ozaki) of `bench_cases/profile_case.py --step --precision mixed --nb 24`
 TRAFFIC_PER_LAUNCH = {("ozaki_kernel", 24): (22806.05e6 + 2227.33e6) / 187}
 TRAFFIC_SOURCE = "ncu capture of all slice-product launches of one 24-trajectory step (mean per launch)"
 

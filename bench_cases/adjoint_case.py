@@ -1,5 +1,5 @@
 """Gradient of a dipole-response objective with respect to pulse parameters, on
-the GPU:  python -m python_code_to_check_c_gb300.adjoint_case
+the GPU:  python bench_cases/adjoint_case.py
     [--workload ccsd_o10_v38] [--method CCSD] [--steps 500] [--dt 0.01] [--bumps 32]
     [--checkpoint 50] [--precision fp64|mixed] [--fd 3] [--store -1|0|1]
 
@@ -15,6 +15,11 @@ differences (h = 1e-5) for the first --fd parameters (A, w0, c_0, ...).
 in half the free device memory (-1, default)."""
 from __future__ import annotations
 
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
 import argparse
 import json
 import time
@@ -22,9 +27,9 @@ import time
 import numpy as np
 import torch
 
-from .engine import CCEngine
-from .pulse import Pulse, cosine_weights, pulse_gradient
-from .system import WORKLOADS, mp2_guess, synthetic_system
+from python_code_to_check_c_gb300.engine import CCEngine
+from python_code_to_check_c_gb300.pulse import Pulse, cosine_weights, pulse_gradient
+from python_code_to_check_c_gb300.system import WORKLOADS, mp2_guess, synthetic_system
 
 
 def main():

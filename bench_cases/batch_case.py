@@ -1,5 +1,5 @@
 """Batched trajectories over uneven systems on one GPU:
-    python -m python_code_to_check_c_gb300.batch_case [--steps 20] [--check-steps 200]
+    python bench_cases/batch_case.py [--steps 20] [--check-steps 200]
         [--systems o8_v30,ccsd_o10_v38,o14_v58,o18_v82] [--no-autotune]
 
 Each system (seeded DF integrals, x/y/z dipoles) gets 24 trajectories -- 3
@@ -14,6 +14,11 @@ trajectories of each system against the FP64 form over --check-steps steps
 (scaled down for the larger systems by --check-budget-s)."""
 from __future__ import annotations
 
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
 import argparse
 import json
 import threading
@@ -22,9 +27,9 @@ import time
 import numpy as np
 import torch
 
-from ._lib import make_field
-from .engine import CCEngine
-from .system import WORKLOADS, mp2_guess, synthetic_system
+from python_code_to_check_c_gb300._lib import make_field
+from python_code_to_check_c_gb300.engine import CCEngine
+from python_code_to_check_c_gb300.system import WORKLOADS, mp2_guess, synthetic_system
 
 AMPS = (0.001, 0.002, 0.005, 0.01)
 W0S = (0.5, 0.923)

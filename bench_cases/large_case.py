@@ -1,5 +1,5 @@
 """Large TD-CCSD / TD-CC2 on one GPU:
-    python -m python_code_to_check_c_gb300.large_case [--workload o24_v160] [--method CCSD]
+    python bench_cases/large_case.py [--workload o24_v160] [--method CCSD]
         [--mixed-steps 10] [--fp64-steps 2]
 
 Seeded DF integrals (Q = 480 at o=24, v=160; <pq||rs> built on the device by
@@ -16,6 +16,11 @@ every launch (the ladder and ring contractions with their tensor work
 fraction: FP64-equivalent flops x slice products / time / measured BF16 peak)."""
 from __future__ import annotations
 
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
 import argparse
 import json
 import os
@@ -24,9 +29,9 @@ import time
 import numpy as np
 import torch
 
-from ._lib import make_field
-from .engine import CCEngine, profile_step, tei_from_df_device
-from .system import WORKLOADS, mp2_guess_oovv, synthetic_system
+from python_code_to_check_c_gb300._lib import make_field
+from python_code_to_check_c_gb300.engine import CCEngine, profile_step, tei_from_df_device
+from python_code_to_check_c_gb300.system import WORKLOADS, mp2_guess_oovv, synthetic_system
 
 
 def main():

@@ -1,16 +1,21 @@
 """Runs one right-hand side (or one RK4 step) of a named workload on the GPU,
-for profilers:  python -m python_code_to_check_c_gb300.profile_case
+for profilers:  python bench_cases/profile_case.py
     --workload o14_v58 --method CCSD --block T2 [--repeat 2] [--step] [--nb 8]"""
 from __future__ import annotations
+
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 import argparse
 
 import numpy as np
 import torch
 
-from . import _lib
-from .engine import CCEngine
-from .system import WORKLOADS, mp2_guess, synthetic_system
+from python_code_to_check_c_gb300 import _lib
+from python_code_to_check_c_gb300.engine import CCEngine
+from python_code_to_check_c_gb300.system import WORKLOADS, mp2_guess, synthetic_system
 
 
 def main():

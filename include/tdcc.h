@@ -295,9 +295,11 @@ int tdcc_spectrum(const void* mu, long long nsteps, long long stride, double dt,
    every device loading the library keeps until exit; limits o <= 64 and
    v <= 256 (larger: TDCC_ERR_LIMIT).  The first call on a device looks up
    the array's device address (cudaGetSymbolAddress) with that device
-   current; make that first call before any stream capture.  All calls share
-   the one array: calls whose GPU work overlaps (different streams or
-   threads) race and give wrong results -- serialise them.  Inputs as in
+   current; make that first call before any stream capture.  The address is
+   kept for the life of the process: a device reset (cudaDeviceReset) in
+   between is not supported.  All calls share the one array: calls whose GPU
+   work overlaps (different streams or threads) race and give wrong results
+   -- serialise them.  Inputs as in
    tdcc_dipole; mu: device float64 [n_mu][n][n]; mu_out: device
    complex128[n_mu].                                                       */
 int tdcc_dipole_noalloc(int o, int v, const void* t1, const void* t2, const void* l1,

@@ -544,24 +544,26 @@ int fail(int code, const std::string& m) {
 
 // drops the right-hand-side programs (and their workspace) and the captured
 // step graphs; they are rebuilt on next use
+// Every program instance a system can hold: the right-hand sides, the
+// density / dipole program and the reverse-mode programs.  Code that must
+// visit all of them (error flags, resets) goes through this one list.
+std::vector<std::unique_ptr<ProgInst>*> all_programs(tdcc_system s) {
+  std::vector<std::unique_ptr<ProgInst>*> v;
+  for (auto& mrow : s->rhs)
+    for (auto& pi : mrow) v.push_back(&pi);
+  v.push_back(&s->dens);
+  for (auto& mrow : s->adjp)
+    for (auto& pi : mrow) v.push_back(&pi);
+  return v;
+}
+
 void reset_programs(tdcc_system s) {
   cudaDeviceSynchronize();
-  for (auto& mrow : s->rhs)
-    for (auto& pi : mrow)
-      if (pi) {
-        s->ws_bytes -= pi->bytes;
-        pi.reset();
-      }
-  if (s->dens) {
-    s->ws_bytes -= s->dens->bytes;
-    s->dens.reset();
-  }
-  for (auto& mrow : s->adjp)
-    for (auto& pi : mrow)
-      if (pi) {
-        s->ws_bytes -= pi->bytes;
-        pi.reset();
-      }
+  for (auto* slot : all_programs(s))
+    if (*slot) {
+      s->ws_bytes -= (*slot)->bytes;
+      slot->reset();
+    }
   for (auto& g : s->gexec)
     if (g) {
       cudaGraphExecDestroy(g);
@@ -940,21 +942,20 @@ int tdcc_check_errors(tdcc_system s) {
   if (!s) return fail(TDCC_ERR_ARG, "null system");
   const cudaError_t ce = cudaDeviceSynchronize();
   if (ce != cudaSuccess) return fail(TDCC_ERR_CUDA, std::string("device error: ") + cudaGetErrorString(ce));
-  for (int m = 0; m < 2; ++m)
-    for (int b = 0; b < 9; ++b) {
-      auto& pi = b < 4 ? s->rhs[m][b] : s->adjp[m][b - 4];
-      if (!pi || pi->prog->err_slot < 0) continue;
-      int flag = 0;
-      void* p = pi->bases[pi->prog->err_slot];
-      if (cudaMemcpy(&flag, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return fail(TDCC_ERR_CUDA, "reading the tensor-core error flag failed");
-      if (flag) {
-        const int zero = 0;
-        cudaMemcpy(p, &zero, sizeof(int), cudaMemcpyHostToDevice);
-        return fail(TDCC_ERR_CUDA, "tensor-core kernel in " + pi->prog->name + " gave up waiting (code " +
-                                       std::to_string(flag) + ")");
-      }
+  for (auto* slot : all_programs(s)) {
+    auto& pi = *slot;
+    if (!pi || pi->prog->err_slot < 0) continue;
+    int flag = 0;
+    void* p = pi->bases[pi->prog->err_slot];
+    if (cudaMemcpy(&flag, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return fail(TDCC_ERR_CUDA, "reading the tensor-core error flag failed");
+    if (flag) {
+      const int zero = 0;
+      cudaMemcpy(p, &zero, sizeof(int), cudaMemcpyHostToDevice);
+      return fail(TDCC_ERR_CUDA, "tensor-core kernel in " + pi->prog->name + " gave up waiting (code " +
+                                     std::to_string(flag) + ")");
     }
+  }
   return TDCC_OK;
 }
 

@@ -999,11 +999,15 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
 
 template <class C>
 static cudaError_t launch_variant(const TcArgs& a0, const void* packA, const void* packB, cudaStream_t st) {
-  // kernel attributes, once per process (engines on several host threads
-  // may launch their first slice products together)
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [] {
+  // kernel attributes act on the current device's context: set them once
+  // per device (engines on several host threads may launch their first
+  // slice products together)
+  constexpr int kMaxDev = 64;
+  static std::once_flag once[kMaxDev];
+  static cudaError_t attr_err[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+  std::call_once(once[dev], [dev] {
     cudaError_t e = cudaFuncSetAttribute(ozaki_kernel<true, true, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(ozaki_kernel<true, false, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
@@ -1024,9 +1028,9 @@ static cudaError_t launch_variant(const TcArgs& a0, const void* packA, const voi
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(ozaki_kernel<false, false, C>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                cudaSharedmemCarveoutMaxShared);
-    attr_err = e;
+    attr_err[dev] = e;
   });
-  if (attr_err != cudaSuccess) return attr_err;
+  if (attr_err[dev] != cudaSuccess) return attr_err[dev];
   TcArgs a = a0;
   if (a.S > C::STAGES) return cudaErrorInvalidValue;  // the ring holds one K block's slices
   int cols = 32;

@@ -36,6 +36,9 @@ __device__ __align__(256) double2 g_dipole_scratch[kScratchElems];
 
 // Device addresses of g_dipole_scratch, one per device (host code cannot use
 // the symbol itself: on the host it is only a stand-in for the device array).
+// Looked up once per device and kept for the life of the process; a device
+// reset (cudaDeviceReset) reloads the module, after which a kept address
+// would be stale, so resetting a device between calls is not supported.
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 double2* g_scratch_addr[kMaxDevices] = {};

@@ -7,7 +7,7 @@ loop body of CCSD_Helper.py:1206-1240 twice -- clongdouble and complex128 --
 from the golden o=4, v=8 ground states, with the reference's field
 Vt(t) = -A mu_z exp(i 2 pi w0 t), 20 steps, precs = 15:
 
-    python tests/golden/make_extended_golden.py [/path/to/reference]
+    python tests/golden/make_extended_golden.py /path/to/reference
 
 Output: ``golden_o4_v8_extended.npz`` (mu_z(t) of both runs, CCSD and CC2).
 """
@@ -52,7 +52,9 @@ def run(h, F, mu_z, st, method, dtype):
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_extended_golden.py <path of the reference checkout>")
+    ref_dir = sys.argv[1]
     mod = mg.load_reference(ref_dir)
     g = np.load(os.path.join(HERE, "golden_o4_v8.npz"))
     sysm = mg.synthetic_system(int(g["o"]), int(g["v"]), int(g["nq"]), int(g["seed"]))

@@ -4,7 +4,7 @@ Run in a container that has the reference checkout (read-only) and
 opt_einsum; psi4 and pandas are replaced by empty stub modules because only
 the integral setup and the CSV writers use them, and neither is exercised:
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference
 
 The helper objects are built with ``__new__`` (skipping the psi4 SCF in
 ``CCSD_Helper.__init__``) and given ``occ``/``vir``/``TEI`` from the seeded
@@ -172,7 +172,9 @@ def ground_and_dynamics(mod, sysm, h, out):
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <path of the reference checkout>")
+    ref_dir = sys.argv[1]
     mod = load_reference(ref_dir)
     cases = [(4, 8, 72, 48, True), (6, 10, 72, 610, False), (3, 5, 40, 35, False)]
     for o, v, nq, seed, full in cases:

@@ -4,7 +4,7 @@ the reference's own integral setup -- ``CCSD_Helper.__init__``, ``TEI_MO``,
 deterministic psi4 stand-in of ``tests/fake_psi4.py`` (psi4 is not installed
 here) and stores what it builds:
 
-    python tests/golden/make_psi4_adapter_golden.py [/path/to/reference]
+    python tests/golden/make_psi4_adapter_golden.py /path/to/reference
 
 Output: ``psi4_adapter_fake.npz`` with the spin-orbital Fock matrix, the three
 dipole matrices, <pq||rs>, the occupied spin-orbital count and the SCF energy.
@@ -41,4 +41,6 @@ def main(ref_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_psi4_adapter_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

@@ -1,6 +1,9 @@
 """Restart / output files in the reference's formats (CCSD_Helper.py:1102-1145,
 CC_Calculator.py:70-135).  CPU only."""
+import os
+
 import numpy as np
+import pytest
 
 from python_code_to_check_c_gb300 import restart_io
 
@@ -77,3 +80,50 @@ def test_save_and_load_restart(tmp_path):
     assert np.array_equal(F2, np.around(F.real, 15))        # the imaginary part of F is dropped
     for x, y in ((a1, t1), (a2, t2), (b1, l1), (b2, l2)):
         assert np.array_equal(x, np.around(y.real, 15) + 1j * np.around(y.imag, 15))
+
+
+# ---- pinned to the reference's own writers (fixture: tests/golden/make_restart_golden.py) ----
+REF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "restart_ref.npz")
+NAMES = ("F", "t1", "t2", "lam1", "lam2")
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return dict(np.load(REF))
+
+
+@pytest.mark.parametrize("precs", [15, 8])
+def test_save_data_files_byte_identical_to_reference(tmp_path, ref, precs):
+    """save_data writes the ten restart files exactly as the reference's
+    write_2data / write_4data (CCSD_Helper.py:1107-1122) write a complex128
+    state (the engine's precision)."""
+    st = {n: ref[f"in_{n}"] for n in NAMES}
+    restart_io.save_data(tmp_path, st["F"], st["t1"], st["t2"], st["lam1"], st["lam2"], [], [], precs, None)
+    for n in NAMES:
+        for part in ("real", "imag"):
+            got = (tmp_path / f"{n}_{part}.dat").read_text()
+            assert got == str(ref[f"f64_p{precs}_{n}_{part}"]), (n, part)
+
+
+@pytest.mark.parametrize("kind", ["f64", "ld"])
+@pytest.mark.parametrize("precs", [15, 8])
+def test_readers_parse_reference_files(tmp_path, ref, kind, precs):
+    """The readers give back the arrays the reference wrote: each value as the
+    nearest float64 to its text (what the reference's convert_2data /
+    convert_4data, CC_Calculator.py:85-113, read back), including files a
+    fresh reference run writes from its extended-precision (longdouble)
+    state; for a complex128 state that is np.around(x, precs) exactly."""
+    o, v = ref["in_t1"].shape
+    for n in NAMES:
+        x = ref[f"in_{n}"]
+        for part, arr in (("real", x.real), ("imag", x.imag)):
+            p = tmp_path / f"{n}_{part}.dat"
+            text = str(ref[f"{kind}_p{precs}_{n}_{part}"])
+            p.write_text(text)
+            got = restart_io.read_2data(p, *x.shape) if x.ndim == 2 else restart_io.read_4data(p, o, v)
+            want = np.array([float(line.split("\t")[-1]) for line in text.splitlines()]).reshape(x.shape)
+            assert np.array_equal(got, want), (n, part)
+            if kind == "f64":
+                assert np.array_equal(got, np.around(arr, precs)), (n, part)
+            else:
+                assert np.abs(got - np.around(arr, precs)).max() <= 10.0 ** -precs
