@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--method", default="CCSD", choices=["CCSD", "CC2"])
     p.add_argument("--nb", type=int, default=24, help="trajectories advanced together (24 = 3 pol x 4 A x 2 w0)")
     p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--slices", type=int, default=5, help="BF16 slices per operand in the mixed form")
+    p.add_argument("--fp64-batch-steps", type=int, default=4, help="timed steps of the batched FP64 form")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--adjoint-steps", type=int, default=100, help="pulse-gradient cost measurement (0: skip)")
     return p.parse_args()
@@ -132,12 +134,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def cpu_oracle_rate(sysm, method, state, budget_s=12.0, max_steps=50):
-    """Oracle (numpy restatement of the reference) RK4 steps/s on the host cores,
-    the z / A=0.002 / w0=0.923 trajectory."""
+def cpu_oracle_rate(sysm, method, state, budget_s=12.0, max_steps=50, traj=REF_TRAJ):
+    """Oracle (numpy restatement of the reference) RK4 steps/s on the host cores
+    for one trajectory (default: z / A=0.002 / w0=0.923)."""
     from oracle.cc_oracle import CCOracle, sin_field
     orc = CCOracle(sysm.tei(), sysm.o, mu=sysm.mu)
-    Vt = sin_field(REF_TRAJ[1], REF_TRAJ[2], sysm.mu[REF_TRAJ[0]])
+    Vt = sin_field(traj[1], traj[2], sysm.mu[traj[0]])
     t = 0.0
     s = state
     t0 = time.perf_counter()
@@ -156,24 +158,34 @@ def cpu_oracle_rate(sysm, method, state, budget_s=12.0, max_steps=50):
 _THREAD_VARS = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS")
 
 
-def _one_thread_child(workload, method, state, budget_s, max_steps, q):
+def _one_thread_child(workload, method, state, budget_s, max_steps, warmup, q, traj, barrier):
     from python_code_to_check_c_gb300.system import WORKLOADS, synthetic_system
     sysm = synthetic_system(**WORKLOADS[workload], all_dipoles=True)
-    q.put(cpu_oracle_rate(sysm, method, state, budget_s=budget_s, max_steps=max_steps))
+    if warmup > 0:
+        cpu_oracle_rate(sysm, method, state, budget_s=0.0, max_steps=warmup, traj=traj)
+    barrier.wait(timeout=1800)  # every process starts its timed loop at once
+    q.put(cpu_oracle_rate(sysm, method, state, budget_s=budget_s, max_steps=max_steps, traj=traj))
 
 
-def cpu_oracle_rate_one_thread(workload, method, state, budget_s=12.0, max_steps=20):
-    """The same oracle rate with one BLAS thread: a spawned process whose
-    numpy starts with the thread variables set to 1 (no GPU use there)."""
+def _spawn_one_thread(nproc, workload, method, state, budget_s, max_steps, warmup=1):
+    """`nproc` spawned processes (numpy with one BLAS thread each, no GPU use),
+    process k advancing trajectory k of the batch after `warmup` untimed
+    steps; returns their (steps/s, steps, seconds)."""
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
+    barrier = ctx.Barrier(nproc)
+    trajs = trajectories(nproc)
     saved = {k: os.environ.get(k) for k in _THREAD_VARS}
+    procs = []
     try:
         for k in _THREAD_VARS:
             os.environ[k] = "1"
-        proc = ctx.Process(target=_one_thread_child, args=(workload, method, state, budget_s, max_steps, q))
-        proc.start()
+        for k in range(nproc):
+            pr = ctx.Process(target=_one_thread_child,
+                             args=(workload, method, state, budget_s, max_steps, warmup, q, trajs[k], barrier))
+            pr.start()
+            procs.append(pr)
     finally:
         for k, v in saved.items():
             if v is None:
@@ -181,32 +193,82 @@ def cpu_oracle_rate_one_thread(workload, method, state, budget_s=12.0, max_steps
             else:
                 os.environ[k] = v
     try:
-        res = q.get(timeout=budget_s * 10 + 300)
+        res = [q.get(timeout=budget_s * 10 + 1800) for _ in range(nproc)]
     finally:
-        proc.join(timeout=60)
+        for pr in procs:
+            pr.join(timeout=60)
     return res
 
 
+def cpu_oracle_rate_one_thread(workload, method, state, budget_s=12.0, max_steps=20):
+    """The oracle rate with one BLAS thread: a spawned process whose numpy
+    starts with the thread variables set to 1 (no GPU use there)."""
+    return _spawn_one_thread(1, workload, method, state, budget_s, max_steps)[0]
+
+
+def cpu_oracle_throughput(workload, method, state, budget_s=12.0, max_steps=20, warmup=1):
+    """Throughput of the host cores: one single-thread oracle process per
+    core, each on its own trajectory, all timed at once; trajectory-steps/s
+    is the sum of the processes' rates.  Returns (rate, processes, steps of
+    all processes, longest timed loop in seconds)."""
+    nproc = os.cpu_count() or 1
+    res = _spawn_one_thread(nproc, workload, method, state, budget_s, max_steps, warmup)
+    return sum(r[0] for r in res), nproc, sum(r[1] for r in res), max(r[2] for r in res)
+
+
+def port_calibration(workload):
+    """The reference's own loop body timed against the oracle on a host with
+    the reference checkout (oracle/calibrate_port.py), if recorded."""
+    try:
+        with open(os.path.join(ROOT, "oracle", "port_calibration.json")) as f:
+            data = json.load(f)
+    except (OSError, ValueError):
+        return None
+    out = {k: v for k, v in data.items() if k.split("/")[0] == workload}
+    return out or None
+
+
+def workload_config(args, sysm, world):
+    """The `config` object of both arms' lines (identical for the same flags)."""
+    return {"workload": f"{args.workload}_x{args.nb}", "method": args.method, "o": sysm.o, "v": sysm.v,
+            "nq": sysm.nq, "dt": DT, "trajectories": args.nb,
+            "fields": "A sin(w0 t), 3 pol x A {0.001,0.002,0.005,0.01} x w0 {0.5,0.923}",
+            "value_counts": "trajectory-steps per second (all trajectories of all replicas)",
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (n^4 integrals and per-step workspace > 129 MB), no flush"}
+
+
 def run_reference(args, rank, world):
+    """The reference arm: the oracle (the numpy restatement of the reference;
+    the reference's own source does not travel to the GPU host) on the host
+    cores, at its best throughput: one single-thread process per core, each
+    advancing its own trajectory of the batch, as independent reference runs
+    would.  The single-trajectory all-cores rate is reported beside it."""
     if rank != 0:
         return
     from python_code_to_check_c_gb300.system import WORKLOADS, synthetic_system
     sysm = synthetic_system(**WORKLOADS[args.workload], all_dipoles=True)
     st = mp2_state(sysm)
     cores = os.cpu_count()
+    warm = max(args.warmup, 1)
+    rate, nproc, n, el = cpu_oracle_throughput(args.workload, args.method, st, budget_s=60.0,
+                                               max_steps=max(1, args.steps), warmup=warm)
     cpu_oracle_rate(sysm, args.method, st, budget_s=0.0, max_steps=1)  # warm-up
-    rate, n, el = cpu_oracle_rate(sysm, args.method, st, budget_s=90.0, max_steps=max(1, args.steps))
+    r16, n16, el16 = cpu_oracle_rate(sysm, args.method, st, budget_s=20.0, max_steps=max(1, args.steps))
+    sample = (f"{nproc} single-thread processes (one per host core), each advancing its own trajectory of the "
+              f"batch after {warm} untimed steps: {n} RK4 steps (+dipole) in all, timed loops of "
+              f"{el:.1f} s; numpy complex128 oracle")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": world,
-        "steps": n, "warmup": 1, "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak",
+        "steps": n, "warmup": warm, "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (seeded DF integrals; MP2-guess state: the cost of a step does not depend on it)",
-        "config": {"workload": f"{args.workload}_x{args.nb}", "method": args.method, "o": sysm.o, "v": sysm.v,
-                   "nq": sysm.nq, "dt": DT, "trajectories": args.nb,
-                   "note": "the reference advances one trajectory per run; trajectory-steps/s = steps/s"},
-        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{n} RK4 steps (+dipole) of one {args.workload} trajectory in {el:.1f} s, "
-                                   f"numpy complex128 oracle, BLAS threads = all {cores} host cores"},
+        "config": workload_config(args, sysm, world),
+        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample,
+                         "one_trajectory_all_cores": {"value": r16, "unit": "steps/s", "cores": cores,
+                                                      "sample": f"{n16} RK4 steps of one trajectory in "
+                                                                f"{el16:.1f} s, BLAS threads = {cores}"},
+                         "reference_vs_port": port_calibration(args.workload)},
         "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -284,6 +346,26 @@ def whole_job_rate(world: int, trajectories: int, steps: int, ms: float) -> floa
     return world * trajectories * steps / (ms / 1e3)
 
 
+# Algorithmic flops of one trajectory-step in the reference's convention: the
+# reference's own contract() calls of one loop body (16 right-hand sides and
+# the dipole), each costed by opt_einsum.contract_path (about 2 x
+# multiply-adds), x2 with one complex operand and x4 with two or more
+# (oracle/calibrate_port.py records the count).  The engine's re-associated
+# equations do fewer (HOISTED_FLOPS, the sum of its contractions' flops).
+REF_FLOPS = {("ccsd_o10_v38", "CCSD"): 5.771e10}
+HOISTED_FLOPS = {("ccsd_o10_v38", "CCSD"): 2.13e10}
+
+
+def flops_note(args, value):
+    """Achieved flop rates of the batched step under both conventions."""
+    key = (args.workload, args.method)
+    out = {}
+    for name, table in (("reference_convention", REF_FLOPS), ("hoisted", HOISTED_FLOPS)):
+        if key in table:
+            out[name] = {"flops_per_trajectory_step": table[key], "achieved_tflops": value * table[key] / 1e12}
+    return out or None
+
+
 def timed(fn):
     import torch
     torch.cuda.synchronize()
@@ -318,12 +400,12 @@ def run_ours(args, rank, world, local_rank):
     if prec == "auto":
         prec = "fp64"
         try:
-            eng.set_precision("mixed", 5)
+            eng.set_precision("mixed", args.slices)
             prec = "mixed"
         except _lib.TdccError:
             eng.set_precision("fp64")
     else:
-        eng.set_precision(prec, 5)
+        eng.set_precision(prec, args.slices)
     eng.set_fields(fields, pols)
 
     def barrier():
@@ -362,7 +444,7 @@ def run_ours(args, rank, world, local_rank):
     v64 = k1 / (ms64 / 1e3)
     single_mixed = None
     if prec == "mixed":
-        e1t.set_precision("mixed", 5)
+        e1t.set_precision("mixed", args.slices)
         e1t.propagate(args.method, gs, 0.0, DT, 3, None)
         k1m = max(1, min(args.steps * 2, 100))
         (_, _), ms1m = timed(lambda: e1t.propagate(args.method, gs, 0.0, DT, k1m, None))
@@ -370,10 +452,27 @@ def run_ours(args, rank, world, local_rank):
         e1t.check_errors()
     e1t.close()
     dmu = float((traj[:k1, ref_k] - traj64[:k1]).abs().max().item())
-    fp64 = {"value": world * v64, "unit": "steps/s", "steps": k1, "trajectories": 1,
-            "batched_mixed_over_fp64": value / (world * v64),
-            "max_dmu_vs_fp64_au": dmu, "dmu_steps": k1, "dmu_trajectory": "z, A=0.002, w0=0.923",
-            "slices": 5 if prec == "mixed" else None}
+
+    # ---- the same batch of trajectories in the plain FP64 form ----
+    kb64 = max(1, min(args.steps, args.fp64_batch_steps))
+    e64 = CCEngine.from_system(sysm, nb=nb)
+    e64.set_precision("fp64")
+    e64.set_fields(fields, pols)
+    e64.propagate(args.method, bstate, 0.0, DT, 2, None)
+    (_, trajb64), msb64 = timed(lambda: e64.propagate(args.method, bstate, 0.0, DT, kb64, None))
+    e64.check_errors()
+    e64.close()
+    vb64 = whole_job_rate(world, nb, kb64, max_over_ranks(msb64, world, dev))
+    dmu_b = float((traj[:kb64] - trajb64[:kb64]).abs().max().item())
+    fp64 = {"value": vb64, "unit": "steps/s", "steps": kb64, "trajectories": nb,
+            "batched_mixed_over_fp64": value / vb64,
+            "max_dmu_vs_fp64_au": dmu_b, "dmu_steps": kb64, "dmu_trajectories": f"all {nb}",
+            "one_trajectory": {"value": world * v64, "unit": "steps/s", "steps": k1,
+                               "max_dmu_vs_fp64_au": dmu, "dmu_steps": k1,
+                               "dmu_trajectory": "z, A=0.002, w0=0.923"},
+            "slices": args.slices if prec == "mixed" else None}
+    if single_mixed is not None:
+        single_mixed["single_mixed_over_fp64"] = single_mixed["value"] / v64
 
     # ---- end-to-end through the public API with host buffers ----
     ke = max(1, min(args.e2e_steps, args.steps))
@@ -432,7 +531,7 @@ def run_ours(args, rank, world, local_rank):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    pairs = 15  # slice products per FP64 product with 5 slices (levels 2..6)
+    pairs = args.slices * (args.slices + 1) // 2  # slice products per FP64 product (levels 2..S+1)
     if kern == "ozaki_kernel":
         achieved = dom["flops"] / (dom["ms"] / 1e3) / 1e12
         peak = peaks.get("bf16_tflops", 1900.0)
@@ -467,31 +566,34 @@ def run_ours(args, rank, world, local_rank):
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         host_state = [x.cpu().numpy() for x in gs]
-        rate, n, el = cpu_oracle_rate(sysm, args.method, host_state, budget_s=12.0, max_steps=20)
-        cpu = {"value": rate, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{n} RK4 steps (+dipole) of one {args.workload} trajectory in {el:.1f} s, numpy "
-                         f"complex128 oracle, BLAS threads = all host cores"}
+        rate, nproc, n, el = cpu_oracle_throughput(args.workload, args.method, host_state, budget_s=12.0,
+                                                   max_steps=20, warmup=1)
+        cpu = {"value": rate, "unit": "steps/s", "cores": nproc, "kind": "port",
+               "sample": f"{nproc} single-thread oracle processes (one per host core), each advancing its own "
+                         f"trajectory of the batch: {n} RK4 steps (+dipole) in all, timed loops of {el:.1f} s; "
+                         f"numpy complex128"}
+        r16, n16, el16 = cpu_oracle_rate(sysm, args.method, host_state, budget_s=12.0, max_steps=20)
+        cpu["one_trajectory_all_cores"] = {
+            "value": r16, "unit": "steps/s", "cores": os.cpu_count(),
+            "sample": f"{n16} RK4 steps (+dipole) of one trajectory in {el16:.1f} s, BLAS threads = all host cores"}
         try:
             r1, n1, el1 = cpu_oracle_rate_one_thread(args.workload, args.method, host_state, budget_s=12.0)
             cpu["one_thread"] = {"value": r1, "unit": "steps/s", "cores": 1,
                                  "sample": f"{n1} RK4 steps (+dipole) in {el1:.1f} s, same oracle, one BLAS thread"}
-        except Exception as ex:  # reported, not fatal: the all-cores figure stands
+        except Exception as ex:  # reported, not fatal: the throughput figure stands
             cpu["one_thread"] = {"unavailable": str(ex)[:200]}
+        cpu["reference_vs_port"] = port_calibration(args.workload)
     ws = eng.workspace_bytes()
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == "fp64" else "bf16x5-split+f64",
+        "dtype": "f64" if prec == "fp64" else f"bf16x{args.slices}-split+f64",
         "data": "synthetic (seeded DF integrals, ground state by device DIIS)",
-        "config": {"workload": f"{args.workload}_x{nb}", "method": args.method, "o": sysm.o, "v": sysm.v,
-                   "nq": sysm.nq, "dt": DT, "trajectories": nb,
-                   "fields": "A sin(w0 t), 3 pol x A {0.001,0.002,0.005,0.01} x w0 {0.5,0.923}",
-                   "value_counts": "trajectory-steps (nb per batched step)", "precision": prec,
-                   "parallelism": f"replicas x{world}",
-                   "l2": f"per-step working set {ws / 2**30:.1f} GiB workspace + "
-                         f"{sysm.n ** 4 * 8 / 2**20:.0f} MiB integrals (> 129 MB L2), no flush",
-                   "ground_state": gs_info},
+        "config": workload_config(args, sysm, world),
+        "precision": prec, "ground_state": gs_info,
+        "working_set": f"{ws / 2**30:.1f} GiB workspace + {sysm.n ** 4 * 8 / 2**20:.0f} MiB integrals",
+        "flops": flops_note(args, value),
         "roofline": roof, "kernel_breakdown": breakdown, "top_contractions": top_contractions,
         "cpu_baseline": cpu, "e2e": e2e,
         "fp64_form": fp64, "single_trajectory_mixed": single_mixed, "adjoint": adj,
