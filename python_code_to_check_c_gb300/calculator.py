@@ -27,8 +27,13 @@ the last completed step) are written; reaching ``tf`` writes nothing, as in
 the reference.
 
 ``timing.csv`` rows: ``total`` is the wall time of one step (chunk wall time
-over its steps).  The four blocks of a step run concurrently inside one graph
-and have no separate wall times, so the ``t1 t2 l1 l2`` columns are NaN.
+over its steps), and, as in the reference, the sum of the ``t1 t2 l1 l2``
+columns.  The four blocks of a step run concurrently inside one graph and
+have no separate wall times, so each step's time is split between the
+columns in proportion to the blocks' own device times, measured once per
+propagation by one serial step timed per kernel (``CCEngine.block_times``;
+the reference times ft1/ft2/fL1/fL2 one after another,
+CCSD_Helper.py:1215-1228).
 
 Systems come from psi4 when a psi4 module is passed (``system_from_psi4``),
 or from a ``System`` (e.g. ``synthetic_system``) or a workload name.
@@ -167,6 +172,8 @@ class CC_Calculator:
         self._log("time \t\t mu_z_real \t\t mu_z_real")
         self._log(round(t0, 4), "\t", mua[-1].real, "\t", mua[-1].imag)
         limit = None if timeout is None else 0.9 * float(timeout) * 60.0
+        bt = eng.block_times(method, state, t0, dt, field, precs)
+        shares = [x / sum(bt) for x in bt] if sum(bt) > 0 else [0.25] * 4
         data, timing = [], []
         start = time.time()
         t = t0
@@ -203,7 +210,7 @@ class CC_Calculator:
                 stopped = True
             for j in range(n):
                 data.append((round(times[j], 4), float(mus[j].real), float(mus[j].imag)))
-                timing.append((per_step, np.nan, np.nan, np.nan, np.nan))
+                timing.append((per_step, *(per_step * f for f in shares)))
                 self._log(round(times[j], 4), "\t", mus[j].real, "\t", mus[j].imag)
             t = times[n - 1]
             if stopped:

@@ -118,7 +118,7 @@ __device__ __forceinline__ void balanced_digits(unsigned long long f, int S, int
 // are not written at all: they only feed accumulator rows (A) or columns (B)
 // that the product kernel never stores, and their exponent entries only
 // scale those values, so whatever the buffer holds there is harmless.
-__global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
+__global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
   const int per = p.cplx ? 2 : 1;
   const int z = blockIdx.x / p.rows, m = blockIdx.x - z * p.rows;  // one block per live row
   long long ro = 0;
@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
   const double* src = static_cast<const double*>(p.src);
   constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
   unsigned long long mx = 0;
+#pragma unroll 4
   for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
     long long ko;
     decomp_tc(p.gk, k, ko);
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
       mx = max(mx, bits[e] & kAbs);
   }
   for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
-  __shared__ unsigned long long wmax[8];
+  __shared__ unsigned long long wmax[32];
   if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
   __syncthreads();
   mx = 0;
@@ -170,6 +171,73 @@ __global__ void __launch_bounds__(256) pack_kernel(const PackArgs p) {
     for (int part = 0; part < per; ++part) {
       const unsigned long long f = fixed_point(x[part], e, nbits);
       const bool neg = __double_as_longlong(x[part]) < 0;  // sign bit: no FP64 compare
+      const size_t base = (prow + part) * p.K_pad + k;
+      int qd[TC_MAX_SLICES];
+      balanced_digits(f, p.S, qd);
+#pragma unroll
+      for (int s = 0; s < TC_MAX_SLICES; ++s)
+        if (s < p.S) out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -qd[s] : qd[s]));
+    }
+  }
+}
+
+// Short rows (K_pad <= 32 * KW): one warp per logical row, eight rows per
+// block.  Each lane keeps its KW elements of the row in registers, so the
+// row is read once: the warp takes the exponent with shuffles and cuts the
+// digits from the registers (same exponent, digits and layout as
+// pack_kernel).
+template <int KW>
+__global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
+  const int per = p.cplx ? 2 : 1;
+  const int lane = threadIdx.x & 31;
+  const long long lr = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);  // logical row over all batches
+  if (lr >= (long long)p.nb * p.rows) return;  // warp-uniform
+  const int z = (int)(lr / p.rows), m = (int)(lr - (long long)z * p.rows);
+  long long ro = 0;
+  decomp_tc(p.gr, m, ro);
+  ro += z * p.bs;
+  const double* src = static_cast<const double*>(p.src);
+  constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
+  double x[KW][2];
+  unsigned long long mx = 0;
+#pragma unroll
+  for (int j = 0; j < KW; ++j) {
+    const int k = lane + 32 * j;
+    x[j][0] = x[j][1] = 0.0;
+    if (k < p.K) {
+      long long ko;
+      decomp_tc(p.gk, k, ko);
+      const long long el = ro + ko;
+      if (p.cplx) {
+        const double2 v = *reinterpret_cast<const double2*>(src + 2 * el);
+        x[j][0] = v.x;
+        x[j][1] = v.y;
+      } else {
+        x[j][0] = src[el];
+      }
+    }
+    mx = max(mx, max((unsigned long long)__double_as_longlong(x[j][0]) & kAbs,
+                     (unsigned long long)__double_as_longlong(x[j][1]) & kAbs));
+  }
+  for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+  const int E = (int)(mx >> 52);
+  const int eb = mx != 0 ? (E > 0 ? E - 1022 : -1022) + kExpBias : 0;
+  const size_t prow = (size_t)z * p.rows_pad + (size_t)m * per;
+  if (lane == 0) {
+    p.exps[prow] = eb;
+    if (p.cplx) p.exps[prow + 1] = eb;
+  }
+  const int e = row_exp(eb);
+  const int nbits = 7 * p.S;
+  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
+  const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
+#pragma unroll
+  for (int j = 0; j < KW; ++j) {
+    const int k = lane + 32 * j;
+    if (k >= p.K_pad) break;
+    for (int part = 0; part < per; ++part) {
+      const unsigned long long f = fixed_point(x[j][part], e, nbits);
+      const bool neg = __double_as_longlong(x[j][part]) < 0;
       const size_t base = (prow + part) * p.K_pad + k;
       int qd[TC_MAX_SLICES];
       balanced_digits(f, p.S, qd);
@@ -901,11 +969,13 @@ template <bool AC, bool BC, bool CC>
 static void launch_simt_typed(int tile, const GemmArgs& g, int nb, int S, int p2, int e2, int n2, cudaStream_t st) {
   if (S == 6)
     launch_simt_tile<AC, BC, CC, 6>(tile, g, nb, p2, e2, n2, st);
-  else
+  else if (S == 5)
     launch_simt_tile<AC, BC, CC, 5>(tile, g, nb, p2, e2, n2, st);
+  else
+    launch_simt_tile<AC, BC, CC, 4>(tile, g, nb, p2, e2, n2, st);
 }
 
-bool simt_slices_supported(int K, int S) { return K >= 1 && K <= kSimtMaxK && (S == 5 || S == 6); }
+bool simt_slices_supported(int K, int S) { return K >= 1 && K <= kSimtMaxK && S >= 4 && S <= 6; }
 
 cudaError_t launch_simt_slices(const Op& op, const void* A, const void* B, void* C, cudaStream_t st) {
   GemmArgs g = op.g;
@@ -991,8 +1061,21 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
     return cudaErrorInvalidValue;
   const long long blocks = (long long)p.nb * p.rows;
   if (blocks > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;
-  const int threads = p.K_pad >= 256 ? 256 : ((p.K_pad + 31) / 32) * 32;
-  pack_kernel<<<(unsigned)blocks, threads, 0, st>>>(p);
+  if (p.K_pad <= 256) {
+    // short rows: a warp per row, eight rows per block, one read of the row
+    const unsigned grid = (unsigned)((blocks + 7) / 8);
+    if (p.K_pad <= 64)
+      pack_rows_warp_kernel<2><<<grid, 256, 0, st>>>(p);
+    else if (p.K_pad <= 128)
+      pack_rows_warp_kernel<4><<<grid, 256, 0, st>>>(p);
+    else
+      pack_rows_warp_kernel<8><<<grid, 256, 0, st>>>(p);
+  } else {
+    // long rows: a block per row; few long rows (the K = o v^2 operands)
+    // take more threads per row so that the SMs still fill
+    const int threads = (p.K_pad >= 4096 && blocks < 4 * 152) ? 1024 : 256;
+    pack_kernel<<<(unsigned)blocks, threads, 0, st>>>(p);
+  }
   count_launch();
   return cudaGetLastError();
 }

@@ -295,6 +295,17 @@ class CCEngine:
         traj = traj[: int(nsteps) * self.nb].clone()
         return tuple(st), (traj if self.nb == 1 else traj.view(int(nsteps), self.nb))
 
+    def block_times(self, method: str, state, t_prev: float, dt: float, field, precs: int = 15):
+        """Device milliseconds of the four RK4 blocks (T1, T2, L1, L2: the
+        reference's ft1/ft2/fL1/fL2) in one step from ``state``, each block
+        run alone (one serial, eager step timed per kernel by CUDA events;
+        the state is not advanced)."""
+        ms = [0.0] * 4
+        for r in profile_step(self, method, state, t_prev, dt, field, precs):
+            if 0 <= r["block"] < 4:
+                ms[r["block"]] += r["ms"]
+        return ms
+
 
 def adjoint(eng: "CCEngine", method: str, state, t0: float, dt: float, nsteps: int, weights, field=None,
             precs: int = -1, checkpoint: int = 50, want_state_grad: bool = False):

@@ -29,6 +29,9 @@ class OracleEngine:
         new = self.orc.rk4_step(method, t_prev + dt, dt, st, self.F, self.Vt, precs)
         return tuple(torch.as_tensor(x) for x in new), self.dipole_moment(*new)
 
+    def block_times(self, method, state, t_prev, dt, field, precs=15):
+        return [1.0, 4.0, 2.0, 3.0]
+
     def propagate(self, method, state, t0, dt, n, field, precs=15):
         self.calls.append(("prop", t0, n))
         _, mus, st = self.orc.propagate(method, self.F, [np.asarray(x) for x in state], t0, dt, n, self.Vt, precs)
@@ -43,6 +46,9 @@ class CounterEngine:
 
     def dipole_moment(self, *st):
         return self._mu(st)
+
+    def block_times(self, method, state, t_prev, dt, field, precs=15):
+        return [1.0, 4.0, 2.0, 3.0]
 
     def rk4_step(self, method, state, t_prev, dt, field, precs=15):
         new = tuple(torch.round(x.real) + 1 + 0j for x in state)
@@ -114,6 +120,13 @@ def test_divergence_stop_saves_previous_state(tmp_path):
     assert p["t0"] == 0.01 + 0.01 + 0.01 + 0.01 - 0.01 and (p["i"], p["a"]) == (o, v)
     _, t1, t2, l1, l2 = restart_io.load_restart(str(tmp_path), o, v)
     assert np.all(t1 == 3) and np.all(l2 == 3)     # the state before the stopping step
+    # timing.csv: the block columns split each step's time 1 : 4 : 2 : 3 and sum to total
+    rows = (tmp_path / "timing.csv").read_text().splitlines()
+    assert rows[0] == ",total,t1,t2,l1,l2" and len(rows) == 5
+    for r in rows[1:]:
+        tot, *blk = (float(x) for x in r.split(",")[1:])
+        assert abs(sum(blk) - tot) <= 1e-12 * max(tot, 1e-300)
+        assert np.allclose(np.array(blk) / tot, [0.1, 0.4, 0.2, 0.3])
 
 
 def test_timeout_stop_and_restart(tmp_path):

@@ -37,3 +37,10 @@ def test_tdcc_then_restart(tmp_path, method):
     assert np.array_equal(out2["times"], np.round(times2[1:], 4))
     assert np.abs(out2["mu"] - mus2[1:]).max() < 1e-10
     assert len((tmp_path / "H2O.csv").read_text().splitlines()) == 11
+    # timing.csv: per-step total, split between the four blocks by their device times
+    rows = (tmp_path / "timing.csv").read_text().splitlines()
+    assert rows[0] == ",total,t1,t2,l1,l2" and len(rows) == 11
+    for r in rows[1:]:
+        tot, *blk = (float(x) for x in r.split(",")[1:])
+        assert tot > 0 and all(b > 0 for b in blk)
+        assert abs(sum(blk) - tot) <= 1e-9 * tot

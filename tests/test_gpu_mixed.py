@@ -3,7 +3,7 @@ products (FP32 accumulate), everything else FP64.  Checked against the
 reference's golden residuals and against the FP64 GPU form.
 
 Tolerances (written here, met with S = 5 slices per operand):
-  residuals      relative 1e-9 (max |diff| / max |ref|)
+  residuals      relative 1e-9 (max |diff| / max |ref|); 1e-7 with S = 4
   mu_z(t)        |d mu| <= 1e-8 a.u. over the propagation vs the FP64 form
 """
 import numpy as np
@@ -14,6 +14,7 @@ from golden_util import CASES, load, rel_err
 pytestmark = pytest.mark.gpu
 
 RES_TOL = 1e-9
+RES_TOL4 = 1e-7
 MU_TOL = 1e-8
 
 
@@ -129,12 +130,13 @@ def test_short_contractions_on_the_fp32_pipe(fn, name, args):
         eng.set_simt_policy(64, 0)
         a = (d["t1"], d["t2"]) if args == "t" else (d["t1"], d["t2"], d["l1"], d["l2"])
         errs = []
-        for S in (5, 6):  # the FP32-pipe path takes 5 or 6 slices
+        for S in (4, 5, 6):  # the FP32-pipe path takes 4, 5 or 6 slices
             eng.set_precision("mixed", S)
             got = _np(getattr(eng, fn)(*a, d["F"]))
             errs.append(rel_err(got, d[name]))
-        assert errs[0] < RES_TOL, errs
-        assert errs[0] > errs[1], errs
+        assert errs[0] < RES_TOL4, errs
+        assert errs[1] < RES_TOL, errs
+        assert errs[0] > errs[1] > errs[2], errs
         st = [d["t1"] + 0j, d["t2"] + 0j, d["l1"] + 0j, d["l2"] + 0j]
         recs = profile_step(eng, "CCSD", st, 0.0, 0.01, make_field("sin", 0.002, 0.923))
         assert sum(1 for r in recs if r["kind"] == 0 and r["backend"] == 2) >= 10
