@@ -63,7 +63,7 @@ def parse():
     p.add_argument("--method", default="CCSD", choices=["CCSD", "CC2"])
     p.add_argument("--nb", type=int, default=24, help="trajectories advanced together (24 = 3 pol x 4 A x 2 w0)")
     p.add_argument("--e2e-steps", type=int, default=10)
-    p.add_argument("--slices", type=int, default=5, help="BF16 slices per operand in the mixed form")
+    p.add_argument("--slices", type=int, default=4, help="BF16 slices per operand in the mixed form (4: |d mu| <= 1e-8 over 2000 steps, tests/test_gpu_long.py)")
     p.add_argument("--fp64-batch-steps", type=int, default=4, help="timed steps of the batched FP64 form")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--adjoint-steps", type=int, default=100, help="pulse-gradient cost measurement (0: skip)")

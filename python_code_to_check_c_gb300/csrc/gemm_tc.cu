@@ -728,6 +728,279 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
 }
 
 // ---------------------------------------------------------------------------
+// 128-column tile for S <= 4 slices (TcTile128): one K range per CTA.
+//
+// A tcgen05.mma of 128 x N x 16 costs the same ~71 cycles for every N <= 128,
+// and the TMA unit of an SM delivers about 62 GB/s, so the 64-column tile
+// spends half of its MMA time and 1.5x the loaded bytes per output that a
+// 128-column tile does.  S level accumulators of 128 columns fill TMEM
+// (S <= 4), which leaves no room for int64 partial sums across K chunks:
+// each CTA therefore takes at most one exact chunk of K (the planner splits
+// longer K across CTAs, whose results meet in the output by L2 reductions)
+// and drains TMEM once.  Level sums per K index are at most
+// 2^13 + 2^12 + 2^12 + 2^13 = 24576 (S = 4), so 10 K blocks (640) stay
+// below 2^24 and exact in FP32 (tc_chunk_kblocks).  The drain takes 16
+// columns at a time per warp, stages them in the idle operand ring (one
+// area per warp) and writes them at once, so the whole tile is never staged.
+// ---------------------------------------------------------------------------
+template <bool AC, bool BC>
+__global__ void __launch_bounds__(TcTile128::THREADS, 1)
+    ozaki_tile128_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                         const TcArgs g) {
+  using C = TcTile128;
+  extern __shared__ uint8_t smraw[];
+  uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  uint8_t* stA = sm;                           // STAGES x 16 KB
+  uint8_t* stB = sm + C::STAGES * TC_A_BYTES;  // STAGES x 16 KB
+  TcShared<C>* sh = (TcShared<C>*)(stB + C::STAGES * C::B_BYTES);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = g.S;
+  const int ncols = g.tmem_cols;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < C::STAGES; ++i) {
+      mbar_init(smem_u32(&sh->full[i]), 1);
+      mbar_init(smem_u32(&sh->empty[i]), 1);
+    }
+    mbar_init(smem_u32(&sh->accfull), 1);
+    mbar_init(smem_u32(&sh->accempty), 32 * C::EPI);
+    mbar_init(smem_u32(&sh->done), 1);
+    sh->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    asm volatile("fence.proxy.async.shared::cta;");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = sh->tmem;
+
+  const int mt = g.m_fast ? blockIdx.x : blockIdx.y, nt = g.m_fast ? blockIdx.y : blockIdx.x;
+  const int zb = blockIdx.z / g.nsplit;  // batch
+  const int kb0 = (blockIdx.z - zb * g.nsplit) * g.kb_per_split;
+  const int rowA0 = (g.bat_a ? zb * g.rowsA_pad : 0);
+  const int rowB0 = (g.bat_b ? zb * g.rowsB_pad : 0);
+  const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0;
+      for (int kb = kb0; kb < kb1 && !sh->abort; ++kb)
+        for (int s = 0; s < S && !sh->abort; ++s, ++it) {
+          const int st = it % C::STAGES;
+          const uint32_t ph = (uint32_t)((it / C::STAGES) & 1);
+          if (!mbar_wait(smem_u32(&sh->empty[st]), ph ^ 1u, kWaitLimit)) {
+            fail(sh, g.err, 1);
+            break;
+          }
+          const uint32_t fb = smem_u32(&sh->full[st]);
+          mbar_expect_tx(fb, TC_A_BYTES + C::B_BYTES);
+          tma3d(smem_u32(stA + st * TC_A_BYTES), &tmA, kb * TC_BK, rowA0 + mt * TC_BM, s, fb);
+          tma3d(smem_u32(stB + st * C::B_BYTES), &tmB, kb * TC_BK, rowB0 + nt * C::BN, s, fb);
+        }
+      const int issued = it;
+      for (int j = (issued > C::STAGES ? issued - C::STAGES : 0); j < issued; ++j)
+        mbar_wait(smem_u32(&sh->full[j % C::STAGES]), (uint32_t)((j / C::STAGES) & 1), kWaitLimit);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t id = idesc_bf16(TC_BM, C::BN);
+      int it = 0;
+      bool first = true;
+      for (int kb = kb0; kb < kb1 && !sh->abort; ++kb, it += S) {
+        bool ok = true;
+        for (int s = 0; s < S; ++s) {
+          const int j = it + s;
+          if (!mbar_wait(smem_u32(&sh->full[j % C::STAGES]), (uint32_t)((j / C::STAGES) & 1), kWaitLimit)) {
+            ok = false;
+            break;
+          }
+        }
+        if (!ok) {
+          fail(sh, g.err, 3);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        for (int L = 2; L <= S + 1; ++L) {
+          const uint32_t dacc = tmem + (uint32_t)((L - 2) * C::BN);
+          int np = 0;
+          for (int s = 1; s < L; ++s) {
+            const int t = L - s;
+            if (s > S || t > S) continue;
+            const int sa = (it + s - 1) % C::STAGES, sb = (it + t - 1) % C::STAGES;
+            const uint64_t da = sdesc(smem_u32(stA + sa * TC_A_BYTES));
+            const uint64_t db = sdesc(smem_u32(stB + sb * C::B_BYTES));
+#pragma unroll
+            for (int k = 0; k < TC_BK / 16; ++k) {
+              const uint32_t accf = (first && np == 0 && k == 0) ? 0u : 1u;
+              umma(dacc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), id, accf);
+            }
+            ++np;
+          }
+        }
+        first = false;
+        for (int s = 0; s < S; ++s) umma_commit(smem_u32(&sh->empty[(it + s) % C::STAGES]));
+      }
+      umma_commit(smem_u32(&sh->accfull));
+      umma_commit(smem_u32(&sh->done));
+      mbar_wait(smem_u32(&sh->done), 0, kWaitLimit);
+    }
+  } else {
+    // ---------------- epilogue (warps 2 .. 17) ----------------
+    constexpr int kWq = C::EPI / 4;   // 4 warps per lane quarter
+    constexpr int kCw = C::BN / kWq;  // 32 packed columns per warp
+    const int q = warp & 3;
+    const int hcol = (warp - 2) >> 2;
+    const int row = q * 32 + lane;
+    const int u = 7 * (S + 1);  // S <= 4: sum_L v_L 2^(u - 7L) is exact in int64
+    {
+      const int t = threadIdx.x - 64;
+      constexpr int ncl = BC ? C::BN / 2 : C::BN;
+      if (t < ncl) {
+        const int n = nt * ncl + t;
+        long long o = -1;
+        if (n < g.N) decomp_tc(g.gnC, n, o);
+        sh->col_off[t] = o;
+      }
+      if (t < C::BN) sh->col_exp[t] = row_exp(g.expB[rowB0 + nt * C::BN + t]);
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * C::EPI) : "memory");
+    }
+    const int prow = mt * TC_BM + row;
+    const int m = AC ? (prow >> 1) : prow;
+    const bool odd = AC && (lane & 1);
+    constexpr int NJ = BC ? 8 : 16;          // logical columns per 16 packed columns
+    constexpr int rows_out = AC ? 16 : 32;    // logical rows of this warp
+    constexpr int RS = NJ + 1;                // staging row stride (double2), padded
+    double2* stage = reinterpret_cast<double2*>(sm) + (size_t)(warp - 2) * (32 * RS);
+    const int lr = AC ? (lane >> 1) : lane;
+    const uint32_t tl = (uint32_t)(q * 32) << 16;
+    bool ok = !__any_sync(0xffffffffu, sh->abort != 0);
+    if (ok) {
+      const bool got = mbar_wait(smem_u32(&sh->accfull), 0u, kWaitLimit);
+      if (!__all_sync(0xffffffffu, got)) {
+        fail(sh, g.err, 4);
+        ok = false;
+      }
+    }
+    if (ok && __any_sync(0xffffffffu, sh->abort != 0)) ok = false;
+    if (ok) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int ea = prow < g.rowsA_pad ? row_exp(g.expA[rowA0 + prow]) : 0;
+      const int ebase = ea - u + (g.alpha_pow2 ? g.alpha_e : 0);
+      const bool neg = g.alpha_pow2 && g.alpha_neg;
+      long long coffm = 0;
+      if (m < g.M) decomp_tc(g.gmC, m, coffm);
+      double2* Cc = static_cast<double2*>(g.C) + (g.cc ? zb * g.bsC : 0);
+      double* Cr = static_cast<double*>(g.C) + (g.cc ? 0 : zb * g.bsC);
+      const int m0w = AC ? ((mt * TC_BM + q * 32) >> 1) : (mt * TC_BM + q * 32);
+      const int nrows = min(rows_out, g.M - m0w);
+      const bool red = g.acc || g.atomic;
+      constexpr int RPP = 32 / NJ;  // rows per store pass
+      constexpr int NPASS = rows_out / RPP;
+      const int lc = lane % NJ, lrw = lane / NJ;
+#pragma unroll 1
+      for (int j0 = hcol * kCw; j0 < (hcol + 1) * kCw; j0 += 16) {
+        long long a16[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) a16[j] = 0;
+#pragma unroll
+        for (int L0 = 2; L0 <= 5; L0 += 2) {
+          if (L0 > S + 1) break;
+          uint32_t lv[2][16];
+#pragma unroll
+          for (int i = 0; i < 2; ++i)
+            if (L0 + i <= S + 1) tmem_ld16_nowait(tmem + tl + (uint32_t)((L0 + i - 2) * C::BN + j0), lv[i]);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            const int L = L0 + i;
+            if (L > S + 1) break;
+            const int shl = u - 7 * L;  // >= 0 for L <= S + 1
+#pragma unroll
+            for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(__uint_as_float(lv[i][j])) << shl;
+          }
+        }
+        __syncwarp();  // the previous group's stores have read the staging area
+#pragma unroll
+        for (int k = 0; k < NJ; ++k) {
+          const int jj = (BC ? j0 / 2 : j0) + k;  // logical column within the tile
+          long long re, im;
+          if constexpr (BC) {
+            const long long x0 = a16[2 * k], x1 = a16[2 * k + 1];
+            if constexpr (AC) {
+              const long long p0 = __shfl_xor_sync(0xffffffffu, x0, 1);
+              const long long p1 = __shfl_xor_sync(0xffffffffu, x1, 1);
+              const long long rr = odd ? p0 : x0, ri = odd ? p1 : x1, ir = odd ? x0 : p0, ii = odd ? x1 : p1;
+              re = rr - ii;
+              im = ri + ir;
+            } else {
+              re = x0;
+              im = x1;
+            }
+          } else {
+            const long long x = a16[k];
+            if constexpr (AC) {
+              const long long p = __shfl_xor_sync(0xffffffffu, x, 1);
+              re = odd ? p : x;
+              im = odd ? x : p;
+            } else {
+              re = x;
+              im = 0;
+            }
+          }
+          if (AC && ((k & 1) != (lane & 1))) continue;
+          const int E = ebase + sh->col_exp[BC ? 2 * jj : jj];
+          double vr, vi;
+          if (g.alpha_pow2) {
+            vr = scaled_i64_to_double(neg ? -re : re, E);
+            vi = scaled_i64_to_double(neg ? -im : im, E);
+          } else {
+            const double dr = scaled_i64_to_double(re, E), di = scaled_i64_to_double(im, E);
+            vr = g.ar * dr - g.ai * di;
+            vi = g.ar * di + g.ai * dr;
+          }
+          stage[lr * RS + k] = make_double2(vr, vi);
+        }
+        __syncwarp();
+        // store the group: every lane owns a (row, column) pair per pass
+        const long long cn = sh->col_off[(BC ? j0 / 2 : j0) + lc];
+#pragma unroll 4
+        for (int p = 0; p < NPASS; ++p) {
+          const int r = p * RPP + lrw;
+          const long long cm = __shfl_sync(0xffffffffu, coffm, (AC ? 2 * r : r) & 31);
+          if (r >= nrows || cn < 0) continue;
+          const long long off = cm + cn;
+          const double2 v = stage[r * RS + lc];
+          if (g.cc) {
+            if (red) {
+              atomicAdd(&Cc[off].x, v.x);
+              atomicAdd(&Cc[off].y, v.y);
+            } else {
+              Cc[off] = v;
+            }
+          } else {
+            if (red)
+              atomicAdd(&Cr[off], v.x);
+            else
+              Cr[off] = v.x;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+// ---------------------------------------------------------------------------
 // Short contractions (K <= 64) of the mixed mode on the FP32 pipe: the same
 // exact slice products as the tensor-core path, without packing.  One output
 // tile per block: the block takes the binary exponents of its rows of A and
@@ -1142,8 +1415,53 @@ static cudaError_t launch_variant(const TcArgs& a0, const void* packA, const voi
   return cudaGetLastError();
 }
 
+static cudaError_t launch_tile128(const TcArgs& a0, const void* packA, const void* packB, cudaStream_t st) {
+  using C = TcTile128;
+  constexpr int kMaxDev = 64;
+  static std::once_flag once[kMaxDev];
+  static cudaError_t attr_err[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+  std::call_once(once[dev], [dev] {
+    cudaError_t e = cudaSuccess;
+    for (auto fn : {ozaki_tile128_kernel<true, true>, ozaki_tile128_kernel<true, false>,
+                    ozaki_tile128_kernel<false, true>, ozaki_tile128_kernel<false, false>}) {
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    }
+    attr_err[dev] = e;
+  });
+  if (attr_err[dev] != cudaSuccess) return attr_err[dev];
+  TcArgs a = a0;
+  // one exact K chunk per CTA, S level accumulators of 128 columns
+  if (a.S < 1 || a.S > TC_TILE128_MAX_S || a.S > C::STAGES || a.kb_per_split > tc_chunk_kblocks(a.S))
+    return cudaErrorInvalidValue;
+  int cols = 32;
+  while (cols < a.S * C::BN) cols *= 2;
+  a.tmem_cols = cols;
+  if (a.rowsB_pad % C::BN != 0 || a.rowsA_pad % TC_BM != 0) return cudaErrorInvalidValue;
+  const CUtensorMap ma = slice_map(packA, a.S, (a.bat_a ? a.nb : 1) * a.rowsA_pad, a.kblocks * TC_BK, TC_BM);
+  const CUtensorMap mb = slice_map(packB, a.S, (a.bat_b ? a.nb : 1) * a.rowsB_pad, a.kblocks * TC_BK, C::BN);
+  const unsigned mtiles = (unsigned)(a.rowsA_pad / TC_BM), ntiles = (unsigned)(a.rowsB_pad / C::BN);
+  a.m_fast = (a.rowsA_pad < a.rowsB_pad && ntiles <= 65535u) ? 1 : 0;
+  if ((a.m_fast ? ntiles : mtiles) > 65535u || (long long)a.nb * a.nsplit > 65535LL) return cudaErrorInvalidConfiguration;
+  dim3 grid(a.m_fast ? mtiles : ntiles, a.m_fast ? ntiles : mtiles, (unsigned)((long long)a.nb * a.nsplit));
+  if (a.ac && a.bc)
+    ozaki_tile128_kernel<true, true><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
+  else if (a.ac)
+    ozaki_tile128_kernel<true, false><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
+  else if (a.bc)
+    ozaki_tile128_kernel<false, true><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
+  else
+    ozaki_tile128_kernel<false, false><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st) {
   if (a.nb < 1 || a.nsplit < 1 || (long long)a.nsplit * a.kb_per_split < a.kblocks) return cudaErrorInvalidValue;
+  if (a.variant == 2) return launch_tile128(a, packA, packB, st);
   return a.variant == 1 ? launch_variant<TcNarrow>(a, packA, packB, st) : launch_variant<TcWide>(a, packA, packB, st);
 }
 

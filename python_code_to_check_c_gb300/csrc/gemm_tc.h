@@ -29,5 +29,16 @@ using TcWide = TcCfg<64, 8, 16, 1>;
 // two CTAs per SM (one's drain overlaps the other's MMAs): 32-wide tile, 5
 // stages, 8 drain warps; TMEM (S + 2) x 32 <= 256 columns, so S <= 5
 using TcNarrow = TcCfg<32, 5, 8, 2>;
+// 128-wide tile, one K chunk per CTA (no int64 partial sums): S x 128 <= 512
+// TMEM columns, so S <= 4; 6 stages, 16 drain warps, one CTA per SM
+using TcTile128 = TcCfg<128, 6, 16, 1>;
+constexpr int TC_TILE128_MAX_S = 4;
+
+// K blocks one CTA of the 128-wide tile may accumulate exactly: the FP32
+// level sums grow by at most sum_{s+t=L} |q_s| |q_t| per K index (|q_1| <=
+// 128, |q_s| <= 64 for s >= 2) and must stay within 2^24.
+constexpr int tc_chunk_kblocks(int S) {
+  return S <= 2 ? 16 : S == 3 ? (1 << 24) / (20480 * 64) : (1 << 24) / (24576 * 64);
+}
 
 }  // namespace tdcc

@@ -10,6 +10,7 @@
 #include <stdexcept>
 
 #include "engine.h"
+#include "gemm_tc.h"
 
 namespace tdcc {
 
@@ -942,7 +943,12 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
       err_slot = e.slot;
     }
     const bool ac = op.dta == C64, bc = op.dtb == C64;
-    const long long rA = rup(M * (ac ? 2 : 1), BM), rB = rup(N * (bc ? 2 : 1), BN), Kp = rup(K, BK);
+    // S <= 4: the 128-column tile (one K chunk per CTA, K split across CTAs
+    // beyond it) when B has rows enough to fill it
+    const long long nBrows = N * (bc ? 2 : 1);
+    const bool tile128 = S <= TC_TILE128_MAX_S && nBrows >= 96;
+    const long long rA = rup(M * (ac ? 2 : 1), BM), rB = rup(nBrows, tile128 ? TcTile128::BN : BN),
+                    Kp = rup(K, BK);
     // batched products: an operand with a batch stride is packed per batch
     const int nbt = std::max(op.g.nb, 1);
     const int nbA = (nbt > 1 && op.g.bsA != 0) ? nbt : 1, nbB = (nbt > 1 && op.g.bsB != 0) ? nbt : 1;
@@ -1074,13 +1080,15 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     }
     a.acc = op.g.acc;
     // split K so that few output tiles still occupy the SMs: one CTA per SM,
-    // cost = waves x (K blocks per CTA + fixed pipeline/epilogue overhead)
-    const long long ctas = (rB / BN) * (rA / BM) * nbt;
-    long long splits = 1;
+    // cost = waves x (K blocks per CTA + fixed pipeline/epilogue overhead);
+    // the 128-column tile takes at most one exact K chunk per CTA
+    const long long ctas = (rB / (tile128 ? TcTile128::BN : BN)) * (rA / BM) * nbt;
+    const long long min_sp = tile128 ? (a.kblocks + tc_chunk_kblocks(S) - 1) / tc_chunk_kblocks(S) : 1;
+    long long splits = min_sp;
     {
       double best = 1e300;
-      const long long maxs = std::max<long long>(1, std::min<long long>(a.kblocks, 64));
-      for (long long sp = 1; sp <= maxs; ++sp) {
+      const long long maxs = std::max<long long>(min_sp, std::min<long long>(a.kblocks, 64));
+      for (long long sp = min_sp; sp <= maxs; ++sp) {
         const long long waves = (ctas * sp + 151) / 152;
         const long long per = (a.kblocks + sp - 1) / sp;
         const double cost = (double)waves * (double)(per * S + 6);
@@ -1096,7 +1104,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     a.atomic = splits > 1 ? 1 : 0;
     t.zeroed = a.acc || a.atomic;  // split K is allowed (a zero op precedes when not accumulating)
     // short K: the narrow variant (two CTAs per SM overlap their latencies)
-    a.variant = (a.kb_per_split == 1 && S <= 5) ? 1 : 0;
+    a.variant = tile128 ? 2 : (a.kb_per_split == 1 && S <= 5) ? 1 : 0;
     t.bytes = (long long)S * (nbA * rA + nbB * rB) * Kp * 2 + nbt * M * N * elem_bytes(op.dtc);
     t.reads = {pa.pk_dst, pb.pk_dst};
     if (a.acc || a.atomic) t.reads.push_back(op.sc);
