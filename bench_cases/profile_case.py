@@ -1,6 +1,7 @@
 """Runs one right-hand side (or one RK4 step) of a named workload on the GPU,
 for profilers:  python bench_cases/profile_case.py
-    --workload o14_v58 --method CCSD --block T2 [--repeat 2] [--step] [--nb 8]"""
+    --workload o14_v58 --method CCSD --block T2 [--repeat 2] [--step] [--nb 8]
+    [--precision mixed --slices 4]"""
 from __future__ import annotations
 
 import os
@@ -26,11 +27,12 @@ def main():
     p.add_argument("--repeat", type=int, default=2)
     p.add_argument("--step", action="store_true", help="one RK4 step instead of one RHS")
     p.add_argument("--precision", default="fp64")
+    p.add_argument("--slices", type=int, default=4, help="slices per operand in the mixed form")
     p.add_argument("--nb", type=int, default=1, help="trajectories advanced together")
     a = p.parse_args()
     sysm = synthetic_system(**WORKLOADS[a.workload])
     eng = CCEngine.from_system(sysm, nb=a.nb)
-    eng.set_precision(a.precision)
+    eng.set_precision(a.precision, a.slices)
     t2 = mp2_guess(sysm.tei(), sysm.eps(), sysm.o).astype(np.complex128)
     t1 = np.full((sysm.o, sysm.v), 0.01 + 0.005j)
     st = (t1, t2, t1.copy(), t2.copy())

@@ -359,31 +359,30 @@ struct TcShared {
   int col_exp[C::BN];        // exponent of each packed column of B
 };
 
-// x * 2^E rounded to nearest (ties to even) from the integer's bits: no FP64
-// arithmetic on the normal-range path (GB300's FP64 pipe is narrow).
+// Subnormal or overflowing results (not met by the contractions here) take
+// the FP64 path, out of line so that nothing of it is evaluated on the
+// normal path.
+__device__ __noinline__ double scaled_i64_to_double_rare(long long x, int E) { return ldexp((double)x, E); }
+
+// x * 2^E rounded to nearest (ties to even) from the integer's bits, without
+// branches on the normal-range path and no FP64 arithmetic (GB300's FP64
+// pipe is narrow): the magnitude is normalised to bit 63, its top 53 bits
+// are the significand, the 11 bits below round it, and a carry out of the
+// significand rounds up into the exponent field by the integer addition.
 __device__ __forceinline__ double scaled_i64_to_double(long long x, int E) {
-  if (x == 0) return 0.0;
-  const unsigned long long sgn = x < 0 ? 0x8000000000000000ull : 0ull;
-  const unsigned long long u = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
-  int msb = 63 - __clzll((long long)u);
-  unsigned long long mant;
-  if (msb <= 52) {
-    mant = u << (52 - msb);
-  } else {
-    const int sh = msb - 52;
-    mant = u >> sh;
-    const unsigned long long rem = u & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) {
-      ++mant;
-      if (mant >> 53) {
-        mant >>= 1;
-        ++msb;
-      }
-    }
-  }
-  const int be = msb + E + 1023;
-  if (be <= 0 || be >= 2047) return ldexp((double)x, E);  // subnormal / overflow: rare
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (mant & 0x000FFFFFFFFFFFFFull)));
+  const unsigned long long sgn = (unsigned long long)(x >> 63);  // all ones when negative
+  const unsigned long long u = ((unsigned long long)x ^ sgn) - sgn;
+  if (u == 0ull) return 0.0;
+  const int lz = __clzll((long long)u);
+  const unsigned long long m = u << lz;  // leading one at bit 63
+  const unsigned long long mant = m >> 11;  // 53 bits, leading one at bit 52
+  const unsigned rem = (unsigned)(m & 0x7FFull);
+  const unsigned long long up = (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+  const int be = 63 - lz + E + 1023;  // biased exponent before rounding
+  if (be <= 0 || be >= 2047) return scaled_i64_to_double_rare(x, E);
+  // the leading one of mant adds 1 to the exponent field (be - 1 + 1)
+  const unsigned long long bits = ((unsigned long long)(be - 1) << 52) + mant + up;
+  return __longlong_as_double((long long)(bits | (sgn << 63)));
 }
 
 template <class SH>
@@ -680,7 +679,7 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
       __syncwarp();
       long long coffm = 0;
       if (m < g.M) decomp_tc(g.gmC, m, coffm);
-      double2* C = static_cast<double2*>(g.C) + (g.cc ? zb * g.bsC : 0);
+      double2* Cc = static_cast<double2*>(g.C) + (g.cc ? zb * g.bsC : 0);
       double* Cr = static_cast<double*>(g.C) + (g.cc ? 0 : zb * g.bsC);
       const int m0w = AC ? ((mt * TC_BM + q * 32) >> 1) : (mt * TC_BM + q * 32);
       constexpr int NCW = ncol_log / kWq;  // logical columns of this warp (<= 32)
@@ -707,10 +706,10 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
         const double2 v = stage[r * RS + cc];
         if (g.cc) {
           if (red) {
-            atomicAdd(&C[off].x, v.x);
-            atomicAdd(&C[off].y, v.y);
+            atomicAdd(&Cc[off].x, v.x);
+            atomicAdd(&Cc[off].y, v.y);
           } else {
-            C[off] = v;
+            Cc[off] = v;
           }
         } else {
           if (red)
@@ -739,9 +738,14 @@ __global__ void __launch_bounds__(C::THREADS, C::MINB)
 // longer K across CTAs, whose results meet in the output by L2 reductions)
 // and drains TMEM once.  Level sums per K index are at most
 // 2^13 + 2^12 + 2^12 + 2^13 = 24576 (S = 4), so 10 K blocks (640) stay
-// below 2^24 and exact in FP32 (tc_chunk_kblocks).  The drain takes 16
-// columns at a time per warp, stages them in the idle operand ring (one
-// area per warp) and writes them at once, so the whole tile is never staged.
+// below 2^24 and exact in FP32 (tc_chunk_kblocks).  The ring holds single
+// slices (a 128 x 64 tile of A or of B) with their own barriers: the
+// products of a K block run row by row, (1,1) .. (1,S), (2,1) .., and each
+// slice is released right after its last product, so the TMA (the bound
+// of this tile: about 62 GB/s per SM) keeps loading the next block while
+// the current one finishes.  The drain takes 16 columns at a time per warp,
+// stages them in the idle operand ring (one area per warp) and writes them
+// at once, so the whole tile is never staged.
 // ---------------------------------------------------------------------------
 template <bool AC, bool BC>
 __global__ void __launch_bounds__(TcTile128::THREADS, 1)
@@ -750,9 +754,8 @@ __global__ void __launch_bounds__(TcTile128::THREADS, 1)
   using C = TcTile128;
   extern __shared__ uint8_t smraw[];
   uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  uint8_t* stA = sm;                           // STAGES x 16 KB
-  uint8_t* stB = sm + C::STAGES * TC_A_BYTES;  // STAGES x 16 KB
-  TcShared<C>* sh = (TcShared<C>*)(stB + C::STAGES * C::B_BYTES);
+  uint8_t* ring = sm;  // STAGES slots of 16 KB: one slice of A or of B each
+  TcShared<C>* sh = (TcShared<C>*)(ring + C::STAGES * C::SLOT_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = g.S;
   const int ncols = g.tmem_cols;
@@ -785,67 +788,78 @@ __global__ void __launch_bounds__(TcTile128::THREADS, 1)
   const int rowA0 = (g.bat_a ? zb * g.rowsA_pad : 0);
   const int rowB0 = (g.bat_b ? zb * g.rowsB_pad : 0);
   const int kb1 = min(g.kblocks, kb0 + g.kb_per_split);
+  // Per K block the 2S slices enter the ring in the order A1, B1 .. BS,
+  // A2 .. AS, and the products run row by row, (1,1) .. (1,S), (2,1) ..
+  // (2,S-1), .., (S,1): products start once A1 and B1 have landed, and after
+  // row s both A_s and B_(S+1-s) have had their last use and are released.
+  // Position of a slice within its block: A1 -> 0, B_t -> t, A_s -> S + s - 1.
+  const int per = 2 * S;
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      int it = 0;
+      int j = 0;
       for (int kb = kb0; kb < kb1 && !sh->abort; ++kb)
-        for (int s = 0; s < S && !sh->abort; ++s, ++it) {
-          const int st = it % C::STAGES;
-          const uint32_t ph = (uint32_t)((it / C::STAGES) & 1);
+        for (int i = 0; i < per && !sh->abort; ++i, ++j) {
+          const int st = j % C::STAGES;
+          const uint32_t ph = (uint32_t)((j / C::STAGES) & 1);
           if (!mbar_wait(smem_u32(&sh->empty[st]), ph ^ 1u, kWaitLimit)) {
             fail(sh, g.err, 1);
             break;
           }
           const uint32_t fb = smem_u32(&sh->full[st]);
-          mbar_expect_tx(fb, TC_A_BYTES + C::B_BYTES);
-          tma3d(smem_u32(stA + st * TC_A_BYTES), &tmA, kb * TC_BK, rowA0 + mt * TC_BM, s, fb);
-          tma3d(smem_u32(stB + st * C::B_BYTES), &tmB, kb * TC_BK, rowB0 + nt * C::BN, s, fb);
+          mbar_expect_tx(fb, C::SLOT_BYTES);
+          if (i == 0 || i > S)  // A_1, then A_2 .. A_S
+            tma3d(smem_u32(ring + st * C::SLOT_BYTES), &tmA, kb * TC_BK, rowA0 + mt * TC_BM, i == 0 ? 0 : i - S, fb);
+          else  // B_1 .. B_S
+            tma3d(smem_u32(ring + st * C::SLOT_BYTES), &tmB, kb * TC_BK, rowB0 + nt * C::BN, i - 1, fb);
         }
-      const int issued = it;
-      for (int j = (issued > C::STAGES ? issued - C::STAGES : 0); j < issued; ++j)
-        mbar_wait(smem_u32(&sh->full[j % C::STAGES]), (uint32_t)((j / C::STAGES) & 1), kWaitLimit);
+      const int issued = j;
+      for (int q = (issued > C::STAGES ? issued - C::STAGES : 0); q < issued; ++q)
+        mbar_wait(smem_u32(&sh->full[q % C::STAGES]), (uint32_t)((q / C::STAGES) & 1), kWaitLimit);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       constexpr uint32_t id = idesc_bf16(TC_BM, C::BN);
-      int it = 0;
+      int j0 = 0;
       bool first = true;
-      for (int kb = kb0; kb < kb1 && !sh->abort; ++kb, it += S) {
+      for (int kb = kb0; kb < kb1 && !sh->abort; ++kb, j0 += per) {
         bool ok = true;
-        for (int s = 0; s < S; ++s) {
-          const int j = it + s;
-          if (!mbar_wait(smem_u32(&sh->full[j % C::STAGES]), (uint32_t)((j / C::STAGES) & 1), kWaitLimit)) {
+        for (int s = 1; s <= S && ok; ++s) {
+          const int ja = j0 + (s == 1 ? 0 : S + s - 1);  // A_s
+          if (!mbar_wait(smem_u32(&sh->full[ja % C::STAGES]), (uint32_t)((ja / C::STAGES) & 1), kWaitLimit)) {
             ok = false;
             break;
           }
+          const uint64_t da = sdesc(smem_u32(ring + (ja % C::STAGES) * C::SLOT_BYTES));
+          for (int t = 1; t <= S + 1 - s; ++t) {
+            const int jb = j0 + t;  // B_t
+            if (s == 1 &&
+                !mbar_wait(smem_u32(&sh->full[jb % C::STAGES]), (uint32_t)((jb / C::STAGES) & 1), kWaitLimit)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint64_t db = sdesc(smem_u32(ring + (jb % C::STAGES) * C::SLOT_BYTES));
+            const uint32_t dacc = tmem + (uint32_t)((s + t - 2) * C::BN);
+#pragma unroll
+            for (int k = 0; k < TC_BK / 16; ++k) {
+              // the first product of each level (s = 1) in the first K block starts its accumulator
+              const uint32_t accf = (first && s == 1 && k == 0) ? 0u : 1u;
+              umma(dacc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), id, accf);
+            }
+          }
+          if (!ok) break;
+          // A_s and B_(S+1-s) have had their last use: free their slots
+          umma_commit(smem_u32(&sh->empty[ja % C::STAGES]));
+          umma_commit(smem_u32(&sh->empty[(j0 + S + 1 - s) % C::STAGES]));
         }
         if (!ok) {
           fail(sh, g.err, 3);
           break;
         }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        for (int L = 2; L <= S + 1; ++L) {
-          const uint32_t dacc = tmem + (uint32_t)((L - 2) * C::BN);
-          int np = 0;
-          for (int s = 1; s < L; ++s) {
-            const int t = L - s;
-            if (s > S || t > S) continue;
-            const int sa = (it + s - 1) % C::STAGES, sb = (it + t - 1) % C::STAGES;
-            const uint64_t da = sdesc(smem_u32(stA + sa * TC_A_BYTES));
-            const uint64_t db = sdesc(smem_u32(stB + sb * C::B_BYTES));
-#pragma unroll
-            for (int k = 0; k < TC_BK / 16; ++k) {
-              const uint32_t accf = (first && np == 0 && k == 0) ? 0u : 1u;
-              umma(dacc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), id, accf);
-            }
-            ++np;
-          }
-        }
         first = false;
-        for (int s = 0; s < S; ++s) umma_commit(smem_u32(&sh->empty[(it + s) % C::STAGES]));
       }
       umma_commit(smem_u32(&sh->accfull));
       umma_commit(smem_u32(&sh->done));
@@ -1435,7 +1449,7 @@ static cudaError_t launch_tile128(const TcArgs& a0, const void* packA, const voi
   if (attr_err[dev] != cudaSuccess) return attr_err[dev];
   TcArgs a = a0;
   // one exact K chunk per CTA, S level accumulators of 128 columns
-  if (a.S < 1 || a.S > TC_TILE128_MAX_S || a.S > C::STAGES || a.kb_per_split > tc_chunk_kblocks(a.S))
+  if (a.S < 1 || a.S > TC_TILE128_MAX_S || 2 * a.S > C::STAGES || a.kb_per_split > tc_chunk_kblocks(a.S))
     return cudaErrorInvalidValue;
   int cols = 32;
   while (cols < a.S * C::BN) cols *= 2;

@@ -30,8 +30,17 @@ using TcWide = TcCfg<64, 8, 16, 1>;
 // stages, 8 drain warps; TMEM (S + 2) x 32 <= 256 columns, so S <= 5
 using TcNarrow = TcCfg<32, 5, 8, 2>;
 // 128-wide tile, one K chunk per CTA (no int64 partial sums): S x 128 <= 512
-// TMEM columns, so S <= 4; 6 stages, 16 drain warps, one CTA per SM
-using TcTile128 = TcCfg<128, 6, 16, 1>;
+// TMEM columns, so S <= 4.  Its ring holds single slices (one 128 x 64 tile
+// of A or of B, 16 KB, SWIZZLE_128B) in 12 slots, each with its own
+// barriers, so that a slice is released after its last product rather than
+// with the whole K block; 16 drain warps; one CTA per SM.
+struct TcTile128 {
+  static constexpr int BN = 128, STAGES = 12, EPI = 16, MINB = 1;
+  static constexpr int SLOT_BYTES = TC_BM * TC_BK * 2;  // 16 KB (A: 128 rows, B: BN = 128 rows)
+  static constexpr int THREADS = 64 + 32 * EPI;
+  // + 1 KB alignment and the barrier block
+  static constexpr int SMEM = 1024 + STAGES * SLOT_BYTES + 2048;
+};
 constexpr int TC_TILE128_MAX_S = 4;
 
 // K blocks one CTA of the 128-wide tile may accumulate exactly: the FP32
