@@ -48,63 +48,13 @@
 
 #include "engine.h"
 #include "gemm_tc.h"
+#include "slice_math.cuh"
 
 namespace tdcc {
 
 // ---------------------------------------------------------------------------
 // packing
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void decomp_tc(const ModeGroup& g, int l, long long& o0) {
-  o0 = 0;
-#pragma unroll
-  for (int q = kMaxModes - 1; q >= 0; --q) {
-    if (q < g.n) {
-      const int d = g.dim[q];
-      const int r = l % d;
-      l /= d;
-      o0 += (long long)r * g.s0[q];
-    }
-  }
-}
-
-// Row exponents are stored biased (e + kExpBias; 0 = all-zero row) so that
-// zero-initialised memory and atomicMax give the maximum directly.
-constexpr int kExpBias = 4096;
-__device__ __forceinline__ int row_exp(int biased) { return biased > 0 ? biased - kExpBias : 0; }
-
-// floor(|x| 2^(nbits - e)) as an integer, from the bits of x (exact; no FP64
-// arithmetic).  Requires |x| < 2^e and nbits <= 56, so the result < 2^nbits.
-__device__ __forceinline__ unsigned long long fixed_point(double x, int e, int nbits) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-  const int E = (int)(u >> 52);
-  if (E == 0) return 0ull;  // zero or subnormal: below every slice
-  const unsigned long long M = (u & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
-  const int sh = E - 1075 - e + nbits;  // |x| = M 2^(E-1075)
-  if (sh >= 0) return M << sh;
-  if (sh <= -64) return 0ull;
-  return M >> (-sh);
-}
-
-// The digits of f < 2^(7S) in balanced form, least significant first:
-// every digit below the top one in [-64, 63] (a digit >= 64 becomes d - 128
-// with a carry into the next), the top one in [0, 128].  The value is f
-// itself, sum_s q[s] 2^(7(S-1-s)), and products of digits stay within 2^14.
-template <int SMAX>
-__device__ __forceinline__ void balanced_digits(unsigned long long f, int S, int (&q)[SMAX]) {
-#pragma unroll
-  for (int i = SMAX - 1; i >= 1; --i)
-    if (i < S) {
-      int d = (int)(f & 127ull);
-      f >>= 7;
-      if (d >= 64) {
-        d -= 128;
-        ++f;
-      }
-      q[i] = d;
-    }
-  q[0] = (int)f;
-}
-
 // One block per logical row (per batch; the real and imaginary rows of a
 // complex row together): pass 1 takes the binary exponent e of the row's
 // max |x| (max = f 2^e, f in [0.5, 1); integer ops on the bit patterns, the
@@ -128,15 +78,29 @@ __global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
   const double* src = static_cast<const double*>(p.src);
   constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
   unsigned long long mx = 0;
-#pragma unroll 4
-  for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
-    long long ko;
-    decomp_tc(p.gk, k, ko);
-    const long long e = ro + ko;
-    if (p.cplx)
-      mx = max(mx, max(bits[2 * e] & kAbs, bits[2 * e + 1] & kAbs));
-    else
-      mx = max(mx, bits[e] & kAbs);
+  // four independent loads in flight per thread (complex elements as one 16-byte load)
+  constexpr int U = 4;
+  for (int k0 = threadIdx.x; k0 < p.K; k0 += U * blockDim.x) {
+    unsigned long long v[U][2];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int k = k0 + j * blockDim.x;
+      v[j][0] = v[j][1] = 0ull;
+      if (k < p.K) {
+        long long ko;
+        decomp_tc(p.gk, k, ko);
+        const long long e = ro + ko;
+        if (p.cplx) {
+          const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(bits + 2 * e);
+          v[j][0] = w.x;
+          v[j][1] = w.y;
+        } else {
+          v[j][0] = bits[e];
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < U; ++j) mx = max(mx, max(v[j][0] & kAbs, v[j][1] & kAbs));
   }
   for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
   __shared__ unsigned long long wmax[32];
@@ -155,28 +119,39 @@ __global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
   const int nbits = 7 * p.S;
   __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
   const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
-  for (int k = threadIdx.x; k < p.K_pad; k += blockDim.x) {
-    double x[2] = {0.0, 0.0};
-    if (k < p.K) {
-      long long ko;
-      decomp_tc(p.gk, k, ko);
-      const long long el = ro + ko;
-      if (p.cplx) {
-        x[0] = src[2 * el];
-        x[1] = src[2 * el + 1];
-      } else {
-        x[0] = src[el];
+  for (int k0 = threadIdx.x; k0 < p.K_pad; k0 += U * blockDim.x) {
+    double x[U][2];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      const int k = k0 + j * blockDim.x;
+      x[j][0] = x[j][1] = 0.0;
+      if (k < p.K) {
+        long long ko;
+        decomp_tc(p.gk, k, ko);
+        const long long el = ro + ko;
+        if (p.cplx) {
+          const double2 w = *reinterpret_cast<const double2*>(src + 2 * el);
+          x[j][0] = w.x;
+          x[j][1] = w.y;
+        } else {
+          x[j][0] = src[el];
+        }
       }
     }
-    for (int part = 0; part < per; ++part) {
-      const unsigned long long f = fixed_point(x[part], e, nbits);
-      const bool neg = __double_as_longlong(x[part]) < 0;  // sign bit: no FP64 compare
-      const size_t base = (prow + part) * p.K_pad + k;
-      int qd[TC_MAX_SLICES];
-      balanced_digits(f, p.S, qd);
 #pragma unroll
-      for (int s = 0; s < TC_MAX_SLICES; ++s)
-        if (s < p.S) out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -qd[s] : qd[s]));
+    for (int j = 0; j < U; ++j) {
+      const int k = k0 + j * blockDim.x;
+      if (k >= p.K_pad) break;
+      for (int part = 0; part < per; ++part) {
+        const unsigned long long f = fixed_point(x[j][part], e, nbits);
+        const bool neg = __double_as_longlong(x[j][part]) < 0;  // sign bit: no FP64 compare
+        const size_t base = (prow + part) * p.K_pad + k;
+        int qd[TC_MAX_SLICES];
+        balanced_digits(f, p.S, qd);
+#pragma unroll
+        for (int s = 0; s < TC_MAX_SLICES; ++s)
+          if (s < p.S) out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -qd[s] : qd[s]));
+      }
     }
   }
 }
@@ -358,32 +333,6 @@ struct TcShared {
   long long col_off[C::BN];  // output offset of each logical column of the tile (-1: outside)
   int col_exp[C::BN];        // exponent of each packed column of B
 };
-
-// Subnormal or overflowing results (not met by the contractions here) take
-// the FP64 path, out of line so that nothing of it is evaluated on the
-// normal path.
-__device__ __noinline__ double scaled_i64_to_double_rare(long long x, int E) { return ldexp((double)x, E); }
-
-// x * 2^E rounded to nearest (ties to even) from the integer's bits, without
-// branches on the normal-range path and no FP64 arithmetic (GB300's FP64
-// pipe is narrow): the magnitude is normalised to bit 63, its top 53 bits
-// are the significand, the 11 bits below round it, and a carry out of the
-// significand rounds up into the exponent field by the integer addition.
-__device__ __forceinline__ double scaled_i64_to_double(long long x, int E) {
-  const unsigned long long sgn = (unsigned long long)(x >> 63);  // all ones when negative
-  const unsigned long long u = ((unsigned long long)x ^ sgn) - sgn;
-  if (u == 0ull) return 0.0;
-  const int lz = __clzll((long long)u);
-  const unsigned long long m = u << lz;  // leading one at bit 63
-  const unsigned long long mant = m >> 11;  // 53 bits, leading one at bit 52
-  const unsigned rem = (unsigned)(m & 0x7FFull);
-  const unsigned long long up = (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
-  const int be = 63 - lz + E + 1023;  // biased exponent before rounding
-  if (be <= 0 || be >= 2047) return scaled_i64_to_double_rare(x, E);
-  // the leading one of mant adds 1 to the exponent field (be - 1 + 1)
-  const unsigned long long bits = ((unsigned long long)(be - 1) << 52) + mant + up;
-  return __longlong_as_double((long long)(bits | (sgn << 63)));
-}
 
 template <class SH>
 __device__ __forceinline__ void fail(SH* sh, int* err, int code) {

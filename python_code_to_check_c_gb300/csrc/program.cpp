@@ -876,6 +876,31 @@ cudaError_t Program::run_dag(const std::vector<void*>& bases, cudaStream_t st, P
 
 static long long rup(long long x, long long m) { return (x + m - 1) / m * m; }
 
+// Merges neighbouring modes of a packing traversal whose strides (s0) make
+// them one run (s0[q] == dim[q+1] * s0[q+1]): the flat index maps to the
+// same offsets, with fewer index divisions in the packing kernels.
+static void merge_pack_modes(ModeGroup& g) {
+  ModeGroup m{};
+  for (int q = 0; q < g.n; ++q) {
+    if (g.dim[q] == 1) continue;
+    if (m.n > 0 && m.s0[m.n - 1] == (long long)g.dim[q] * g.s0[q]) {
+      m.dim[m.n - 1] *= g.dim[q];
+      m.s0[m.n - 1] = g.s0[q];
+    } else {
+      m.dim[m.n] = g.dim[q];
+      m.s0[m.n] = g.s0[q];
+      ++m.n;
+    }
+  }
+  if (m.n == 0) {  // a single element
+    m.n = 1;
+    m.dim[0] = 1;
+    m.s0[0] = 0;
+  }
+  for (int q = 0; q < m.n; ++q) m.s1[q] = m.s0[q];
+  g = m;
+}
+
 void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k, int min_mn, int simt_max_k,
                              long long simt_min_macs) {
   if (prec_mode != 1) return;
@@ -1006,6 +1031,10 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     pb.pk_dt = op.dtb;
     pb.reads = {op.sb};
     pb.bytes = nbB * (N * K * elem_bytes(op.dtb) + (long long)S * rB * Kp * 2);
+    merge_pack_modes(pa.pk.gr);
+    merge_pack_modes(pa.pk.gk);
+    merge_pack_modes(pb.pk.gr);
+    merge_pack_modes(pb.pk.gk);
     // resolve packed slots (reuse an identical, still valid packing)
     bool emit_a = true, emit_b = true;
     auto resolve = [&](Op& pk, const ModeGroup& gr, const ModeGroup& gk, bool k_s1, long long rows,
