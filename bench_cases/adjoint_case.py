@@ -1,7 +1,7 @@
 """Gradient of a dipole-response objective with respect to pulse parameters, on
 the GPU:  python bench_cases/adjoint_case.py
     [--workload ccsd_o10_v38] [--method CCSD] [--steps 500] [--dt 0.01] [--bumps 32]
-    [--checkpoint 50] [--precision fp64|mixed] [--fd 3] [--store -1|0|1]
+    [--checkpoint 50] [--precision fp64|mixed] [--fd 3] [--fd-random 0] [--store -1|0|1]
 
 Pulse E(t) = A sin(w0 t) sum_k c_k phi_k(t), 32 Gaussian bumps spread over the
 propagation (sigma = spacing), c_k ~ U(0.5, 1.5) (seed 4), A = 0.003,
@@ -9,7 +9,9 @@ w0 = 0.923; objective J = sum_n dt cos(0.8 t_n) Re mu_z(t_n); start: the
 ground state (device DIIS, 8 vectors, max residual 1e-10).  Prints one JSON
 line: J, the forward time (captured step graphs), the reverse-mode time (its
 own forward with checkpoints + the backward), their ratio, and central
-differences (h = 1e-5) for the first --fd parameters (A, w0, c_0, ...).
+differences (h = 1e-5) for the first --fd parameters (A, w0, c_0, ...), or,
+with --fd-random K, for A, w0 and K envelope coefficients drawn at random
+(seed 7, without replacement).
 --store: the reverse pass reads the forward intermediates recorded per step
 (1), runs each stage's forward ops again (0), or records them when they fit
 in half the free device memory (-1, default)."""
@@ -42,6 +44,7 @@ def main():
     p.add_argument("--checkpoint", type=int, default=50)
     p.add_argument("--precision", default="fp64")
     p.add_argument("--fd", type=int, default=3)
+    p.add_argument("--fd-random", type=int, default=0)
     p.add_argument("--store", type=int, default=-1)
     a = p.parse_args()
     sysm = synthetic_system(**WORKLOADS[a.workload])
@@ -80,7 +83,11 @@ def main():
     names = ["A", "w0"] + [f"c{k}" for k in range(a.bumps)]
     fd = []
     h = 1e-5
-    for k in range(min(a.fd, len(names))):
+    picks = list(range(min(a.fd, len(names))))
+    if a.fd_random > 0:
+        ks = np.random.default_rng(7).choice(a.bumps, size=min(a.fd_random, a.bumps), replace=False)
+        picks = [0, 1] + sorted(int(k) + 2 for k in ks)
+    for k in picks:
         pp = Pulse(pulse.A, pulse.w0, pulse.c.copy(), pulse.t_first, pulse.spacing, pulse.sigma)
         pm = Pulse(pulse.A, pulse.w0, pulse.c.copy(), pulse.t_first, pulse.spacing, pulse.sigma)
         if k == 0:

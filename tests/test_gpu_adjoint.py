@@ -170,3 +170,48 @@ def test_state_gradient_matches_torch_autograd_o6_v12(method):
     for ours, g in zip(a, grads):
         ref = np.conj(g.numpy())  # torch's gradient of a real J is dJ/dRe z + i dJ/dIm z
         assert np.abs(ours - ref).max() <= 1e-10 * np.abs(ref).max(), np.abs(ours - ref).max() / np.abs(ref).max()
+
+
+@pytest.mark.parametrize("method", ["CCSD", "CC2"])
+def test_pulse_gradient_100_steps_o6_v12(method):
+    """o=6, v=12 (Q=72, seed 612), 100 steps of dt = 0.01 from the MP2-guess
+    state, a pulse of 8 Gaussian envelope bumps, checkpoints every 10 steps:
+    dJ/dA, dJ/dw0 and all eight dJ/dc_k against central differences
+    (h = 1e-5), relative 1e-6 of the largest."""
+    from python_code_to_check_c_gb300.engine import CCEngine
+    from python_code_to_check_c_gb300.pulse import Pulse, cosine_weights, pulse_gradient
+    from python_code_to_check_c_gb300.system import WORKLOADS, mp2_guess, synthetic_system
+    sysm = synthetic_system(**WORKLOADS["o6_v12"])
+    t2 = mp2_guess(sysm.tei(), sysm.eps(), sysm.o).astype(np.complex128)
+    t1 = np.zeros((sysm.o, sysm.v), dtype=np.complex128)
+    st = (t1, t2, t1.copy(), t2.copy())
+    rng = np.random.default_rng(12)
+    n, dt, t0 = 100, 0.01, 0.0
+    spacing = n * dt / 7
+    pulse = Pulse(A=0.03, w0=0.923, c=rng.uniform(0.5, 1.5, 8), t_first=0.0, spacing=spacing, sigma=spacing)
+    w = cosine_weights(t0, dt, n)
+    eng = CCEngine.from_system(sysm)
+    try:
+        J, gA, gw, gc = pulse_gradient(eng, method, st, pulse, t0, dt, n, w, checkpoint=10)
+        assert abs(J - _J(eng, method, st, pulse, t0, dt, n, w)) < 1e-13
+        fd = []
+        for name in ["A", "w0"] + [f"c{k}" for k in range(len(pulse.c))]:
+            pp, pm = (Pulse(pulse.A, pulse.w0, pulse.c.copy(), pulse.t_first, pulse.spacing, pulse.sigma)
+                      for _ in range(2))
+            if name == "A":
+                pp.A += H
+                pm.A -= H
+            elif name == "w0":
+                pp.w0 += H
+                pm.w0 -= H
+            else:
+                k = int(name[1:])
+                pp.c[k] += H
+                pm.c[k] -= H
+            fd.append((_J(eng, method, st, pp, t0, dt, n, w) - _J(eng, method, st, pm, t0, dt, n, w)) / (2 * H))
+        ours = np.array([gA, gw] + list(gc))
+        fd = np.array(fd)
+        print(method, "max |adjoint - FD| / max |FD|:", np.abs(ours - fd).max() / np.abs(fd).max())
+        assert np.abs(ours - fd).max() <= 1e-6 * np.abs(fd).max(), (ours, fd)
+    finally:
+        eng.close()
