@@ -8,20 +8,23 @@ Headline workload (``value``): the mixed-precision batched form at o=10,
 v=38 (Q=144 seeded density-fitting integrals), 24 trajectories advanced
 together -- 3 polarisations x A in {0.001, 0.002, 0.005, 0.01} x w0 in
 {0.5, 0.923}, E(t) = A sin(w0 t), dt = 0.005 -- from the converged ground
-state (device DIIS, 8 vectors, max residual 1e-10).  ``value`` counts
-trajectory-steps per second.  The same line reports the plain FP64 GPU form
-(one trajectory, the reference's arithmetic), the mixed form on one
-trajectory, |d mu| of the z / A=0.002 / w0=0.923 trajectory against the FP64
-form, the end-to-end rate with host buffers, the roofline of the dominant
-kernel, the cost of a pulse gradient by reverse mode relative to the forward
-(``adjoint``, FP64, --adjoint-steps steps) and the CPU oracle on the host cores.
+state (device DIIS, 8 vectors, max residual 1e-10), 4 BF16 slices per
+operand (--slices).  ``value`` counts trajectory-steps per second.  The same
+line reports the plain FP64 GPU form on the same 24 trajectories (and on one
+trajectory), the mixed form on one trajectory, |d mu| against the FP64 form,
+the end-to-end rate with host buffers, the roofline of the dominant kernel,
+the achieved flop rates under the reference's flop count and the engine's,
+the cost of a pulse gradient by reverse mode relative to the forward
+(``adjoint``, FP64, --adjoint-steps steps) and the CPU oracle on the host
+cores (one single-thread process per core, each on its own trajectory).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--precision fp64|mixed|auto] [--workload NAME] [--method CCSD|CC2] [--nb 24]
 
 Prints one JSON line (rank 0).  The reference arm (--impl reference) times the
-CPU oracle (the numpy restatement of the reference, all host cores) on the
-same workload, one trajectory at a time as the reference runs them.
+CPU oracle (the numpy restatement of the reference) on the host cores for
+the same workload: one single-thread process per core, each advancing its
+own trajectory of the batch, as independent runs of the reference would.
 """
 from __future__ import annotations
 
@@ -45,11 +48,15 @@ AMPS = (0.001, 0.002, 0.005, 0.01)
 W0S = (0.5, 0.923)
 POLS = (0, 1, 2)
 REF_TRAJ = (2, 0.002, 0.923)  # the single-trajectory configuration (z, A, w0)
-# DRAM bytes (read + write) per launch of the slice-product kernel, averaged over the 187
-# launches of one 24-trajectory step: a single-pass ncu capture (dram__bytes_read.sum,
-# dram__bytes_write.sum, -k regex:ozaki) of `bench_cases/profile_case.py --step --precision mixed --nb 24`
-TRAFFIC_PER_LAUNCH = {("ozaki_kernel", 24): (22806.05e6 + 2227.33e6) / 187}
-TRAFFIC_SOURCE = "ncu capture of all slice-product launches of one 24-trajectory step (mean per launch)"
+# DRAM traffic of the slice-product kernels against their algorithmic bytes (packed operands
+# read once, output written once): 460.9 MB over 403.8 MB for four launches of the T2 program
+# (ladder, 24 batched products, two long-K products), a one-pass ncu capture (dram__bytes_read.sum,
+# dram__bytes_write.sum) of `bench_cases/profile_case.py --block T2 --precision mixed --slices 4
+# --nb 24`; the roofline's traffic per launch is this ratio times the step's algorithmic bytes per
+# slice-product launch.
+TRAFFIC_RATIO = {"ozaki_kernel": 460.9 / 403.8}
+TRAFFIC_SOURCE = ("ncu DRAM bytes / algorithmic bytes of four slice-product launches of the T2 program "
+                  "(1.14), times the step's algorithmic bytes per launch")
 
 
 def parse():
@@ -547,7 +554,7 @@ def run_ours(args, rank, world, local_rank):
         achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "hbm", "unit": "GB/s", "peak_source": "measured HBM copy (MEASURED_PEAKS.json)"}
-    traffic = TRAFFIC_PER_LAUNCH.get((kern, nb))
+    traffic = TRAFFIC_RATIO[kern] * dom["bytes"] / dom["n"] if kern in TRAFFIC_RATIO else None
     roof.update({"kernel": kern, "achieved": achieved, "peak": peak, "frac": achieved / peak,
                  "traffic": traffic,
                  "traffic_source": TRAFFIC_SOURCE if traffic else None,

@@ -1,6 +1,6 @@
 """Large TD-CCSD / TD-CC2 on one GPU:
     python bench_cases/large_case.py [--workload o24_v160] [--method CCSD]
-        [--mixed-steps 10] [--fp64-steps 2]
+        [--mixed-steps 10] [--fp64-steps 2] [--slices 4] [--also-slices 5] [--dt 0.005]
 
 Seeded DF integrals (Q = 480 at o=24, v=160; <pq||rs> built on the device by
 tdcc_tei_from_df, its time against the host numpy build reported with
@@ -41,6 +41,10 @@ def main():
     p.add_argument("--mixed-steps", type=int, default=10)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--host-build", action="store_true")
+    p.add_argument("--slices", type=int, default=4, help="slices per operand in the mixed form")
+    p.add_argument("--dt", type=float, default=0.005, help="time step (a step costs the same for any dt)")
+    p.add_argument("--min-scale", type=float, default=1e-6, help="smallest state scale tried")
+    p.add_argument("--also-slices", type=int, nargs="*", default=[], help="further slice counts timed and compared")
     a = p.parse_args()
     t_build = time.perf_counter()
     sysm = synthetic_system(**WORKLOADS[a.workload])
@@ -71,28 +75,36 @@ def main():
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        _, traj = eng.propagate(a.method, st, 0.0, 0.005, steps, f)
+        _, traj = eng.propagate(a.method, st, 0.0, a.dt, steps, f)
         e1.record()
         torch.cuda.synchronize()
         return traj, e0.elapsed_time(e1) / 1e3
 
-    eng.set_precision("mixed", 5)
+    eng.set_precision("mixed", a.slices)
     while True:
         try:
-            eng.propagate(a.method, st, 0.0, 0.005, 1, f)
+            eng.propagate(a.method, st, 0.0, a.dt, 1, f)
             trmx, smx = timed(a.mixed_steps)
             break
         except Exception:
-            if scale < 1e-6:
+            if scale * 0.1 < a.min_scale:
                 raise
             scale *= 0.1
             st[1] = t2_dev * scale
             st[3] = st[1].clone()
     eng.check_errors()
-    recs = profile_step(eng, a.method, st, 0.0, 0.005, f)
+    recs = profile_step(eng, a.method, st, 0.0, a.dt, f)
     ws_mixed = eng.workspace_bytes()
+    # further slice counts on the same state (rates and |d mu| against the same FP64 steps)
+    more = {}
+    for S2 in a.also_slices:
+        eng.set_precision("mixed", S2)
+        eng.propagate(a.method, st, 0.0, a.dt, 1, f)
+        tr2, s2 = timed(a.mixed_steps)
+        eng.check_errors()
+        more[S2] = (tr2, a.mixed_steps / s2)
     eng.set_precision("fp64")
-    eng.propagate(a.method, st, 0.0, 0.005, 1, f)
+    eng.propagate(a.method, st, 0.0, a.dt, 1, f)
     tr64, s64 = timed(a.fp64_steps)
     k = min(a.fp64_steps, a.mixed_steps)
     dmu = float((trmx[:k] - tr64[:k]).abs().max().item())
@@ -111,10 +123,11 @@ def main():
         x[1] += r["flops"]
         x[2] += 1
     tot = sum(r["ms"] for r in recs)
+    pairs = a.slices * (a.slices + 1) // 2  # slice products per FP64 product
     top = sorted(agg.items(), key=lambda kv: -kv[1][0])[:8]
     contractions = [{"op": tag, "tensor_cores": bool(be), "launches": n, "share_of_step": ms / tot,
                      "fp64_equiv_tflops": fl / (ms / 1e3) / 1e12,
-                     "tensor_work_frac": (fl * 15 / (ms / 1e3) / 1e12 / peak) if be else None}
+                     "tensor_work_frac": (fl * pairs / (ms / 1e3) / 1e12 / peak) if be == 1 else None}
                     for (tag, be), (ms, fl, n) in top]
     print(json.dumps({
         "workload": a.workload, "method": a.method, "o": sysm.o, "v": sysm.v, "nq": sysm.nq,
@@ -123,6 +136,9 @@ def main():
         "mixed_steps_per_s": a.mixed_steps / smx, "mixed_steps": a.mixed_steps,
         "fp64_steps_per_s": a.fp64_steps / s64, "fp64_steps": a.fp64_steps,
         "mixed_over_fp64": (a.mixed_steps / smx) / (a.fp64_steps / s64), "max_dmu_au": dmu, "dmu_steps": k,
+        "slices": a.slices, "dt": a.dt,
+        "also": [{"slices": S2, "mixed_steps_per_s": r2, "mixed_over_fp64": r2 / (a.fp64_steps / s64),
+                  "max_dmu_au": float((t2m[:k] - tr64[:k]).abs().max().item())} for S2, (t2m, r2) in more.items()], "mu_fp64_range": [float(tr64[:k].real.min().item()), float(tr64[:k].real.max().item())],
         "workspace_gb_mixed": ws_mixed / 1e9, "serial_step_ms_mixed": tot, "top_contractions": contractions}))
     eng.close()
 
