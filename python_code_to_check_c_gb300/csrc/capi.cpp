@@ -1216,9 +1216,10 @@ int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, con
           const double t_cur = time_op(pi, op);
           double best = t_cur;
           TcArgs best_a = op.tc;
-          for (int variant = 0; variant < 3; ++variant) {
+          for (int variant = 0; variant < 4; ++variant) {
             if (variant == 1 && op.tc.S > TcNarrow::STAGES) continue;
             if (variant == 2 && (op.tc.S > TC_TILE128_MAX_S || op.tc.rowsB_pad % TcTile128::BN != 0)) continue;
+            if (variant == 3 && op.tc.S > TC_TILE128_MAX_S) continue;
             for (int sp : {0, 1, 2, 3, 4, 6, 8, 12, 16, 24, 32}) {  // 0: the current split
               Op c = op;
               c.tc.variant = variant;
@@ -1230,8 +1231,8 @@ int tdcc_autotune(tdcc_system s, int method, const void* t1, const void* t2, con
                 if (c.tc.nsplit == op.tc.nsplit) continue;
                 if (!c.tc.atomic && !c.tc.acc) continue;  // plain store needs one writer per element
               }
-              // the 128-column tile accumulates at most one exact K chunk per CTA
-              if (variant == 2 && c.tc.kb_per_split > tc_chunk_kblocks(c.tc.S)) continue;
+              // the 128-column and persistent tiles accumulate at most one exact K chunk each
+              if ((variant == 2 || variant == 3) && c.tc.kb_per_split > tc_chunk_kblocks(c.tc.S)) continue;
               if (c.tc.variant == op.tc.variant && c.tc.nsplit == op.tc.nsplit) continue;
               const double t = time_op(pi, c);
               if (t < best * 0.97) {

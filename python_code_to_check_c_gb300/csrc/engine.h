@@ -154,7 +154,7 @@ struct TcArgs {
   int M, N;                 // logical output extents (per batch)
   int rowsA_pad, rowsB_pad; // packed rows per batch
   int nb, nsplit;           // blockIdx.z = batch * nsplit + split
-  int variant;              // 0: 64-wide tile, one CTA per SM; 1: 32-wide, two per SM
+  int variant;              // 0: 64-wide tile, one CTA per SM; 1: 32-wide, two per SM; 2: 128-wide; 3: persistent 64-wide
   int m_fast;               // launch order: M tiles fastest (set by the launcher)
   int bat_a, bat_b;         // A / B packed per batch (else shared by all batches)
   long long bsC;            // output batch stride in elements

@@ -38,6 +38,7 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <map>
@@ -964,6 +965,347 @@ __global__ void __launch_bounds__(TcTile128::THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
+// Persistent 64-column form for S <= 4 slices (TcPersist).  One CTA per SM
+// walks the output tiles t = blockIdx.x, blockIdx.x + gridDim.x, ... (each
+// at most one exact K chunk, as in the 128-column form).  Two TMEM buffers of
+// S level accumulators: the MMA issuer fills buffer j & 1 for its j-th tile
+// once the drain warps have released it (accempty), the drain warps empty it
+// once its MMAs are complete (accfull) and release it as soon as the levels
+// are in registers, before they convert and store -- so a tile's drain runs
+// under the next tile's loads and MMAs.  A and B slices have rings of their
+// own (A1 .. AS and B1 .. BS per K block, products row by row, each slice
+// released after its last product).
+// ---------------------------------------------------------------------------
+struct PersistShared {
+  uint64_t fullA[TcPersist::RA], emptyA[TcPersist::RA];
+  uint64_t fullB[TcPersist::RB], emptyB[TcPersist::RB];
+  uint64_t accfull[2], accempty[2], done;
+  uint32_t tmem;
+  volatile int abort;
+  int stop;                                 // the drain warps' common decision for a tile
+  long long col_off[TcPersist::BN / 1];     // output offset of each logical column (-1: outside)
+  int col_exp[TcPersist::BN];
+};
+
+struct TileCoord {
+  int mt, nt, zb, kb0, kb1, rowA0, rowB0;
+};
+
+__device__ __forceinline__ TileCoord persist_tile(const TcArgs& g, int t, int mtiles, int ntiles) {
+  TileCoord c;
+  const int per = mtiles * ntiles;
+  const int zs = t / per, rem = t - zs * per;
+  if (g.m_fast) {
+    c.mt = rem % mtiles;
+    c.nt = rem / mtiles;
+  } else {
+    c.nt = rem % ntiles;
+    c.mt = rem / ntiles;
+  }
+  c.zb = zs / g.nsplit;
+  c.kb0 = (zs - c.zb * g.nsplit) * g.kb_per_split;
+  c.kb1 = min(g.kblocks, c.kb0 + g.kb_per_split);
+  c.rowA0 = g.bat_a ? c.zb * g.rowsA_pad : 0;
+  c.rowB0 = g.bat_b ? c.zb * g.rowsB_pad : 0;
+  return c;
+}
+
+template <bool AC, bool BC>
+__global__ void __launch_bounds__(TcPersist::THREADS, 1)
+    ozaki_persist_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                         const TcArgs g, int ntiles_total) {
+  using C = TcPersist;
+  extern __shared__ uint8_t smraw[];
+  uint8_t* sm = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  uint8_t* ringA = sm;                                   // RA x 16 KB
+  uint8_t* ringB = ringA + C::RA * C::A_SLOT;            // RB x 8 KB
+  uint8_t* stg = ringB + C::RB * C::B_SLOT;              // EPI x STAGE_WARP
+  PersistShared* sh = (PersistShared*)(stg + C::EPI * C::STAGE_WARP);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = g.S;
+  const int ncols = g.tmem_cols;
+  const int mtiles = g.rowsA_pad / TC_BM, ntiles = g.rowsB_pad / C::BN;
+  const uint32_t buf_cols = (uint32_t)(S * C::BN);  // one buffer of S levels
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < C::RA; ++i) {
+      mbar_init(smem_u32(&sh->fullA[i]), 1);
+      mbar_init(smem_u32(&sh->emptyA[i]), 1);
+    }
+    for (int i = 0; i < C::RB; ++i) {
+      mbar_init(smem_u32(&sh->fullB[i]), 1);
+      mbar_init(smem_u32(&sh->emptyB[i]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&sh->accfull[b]), 1);
+      mbar_init(smem_u32(&sh->accempty[b]), 32 * C::EPI);
+    }
+    mbar_init(smem_u32(&sh->done), 1);
+    sh->abort = 0;
+    sh->stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    asm volatile("fence.proxy.async.shared::cta;");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = sh->tmem;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int ja = 0, jb = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles_total && ok && !sh->abort; t += gridDim.x) {
+        const TileCoord c = persist_tile(g, t, mtiles, ntiles);
+        for (int kb = c.kb0; kb < c.kb1 && ok && !sh->abort; ++kb)
+          for (int i = 0; i < 2 * S; ++i) {
+            const bool isA = i == 0 || i > S;  // A1, B1 .. BS, A2 .. AS
+            const int j = isA ? ja : jb, R = isA ? C::RA : C::RB;
+            const int st = j % R;
+            const uint32_t ph = (uint32_t)((j / R) & 1);
+            const uint32_t eb = smem_u32(isA ? &sh->emptyA[st] : &sh->emptyB[st]);
+            if (!mbar_wait(eb, ph ^ 1u, kWaitLimit)) {
+              fail(sh, g.err, 1);
+              ok = false;
+              break;
+            }
+            const uint32_t fb = smem_u32(isA ? &sh->fullA[st] : &sh->fullB[st]);
+            if (isA) {
+              mbar_expect_tx(fb, C::A_SLOT);
+              tma3d(smem_u32(ringA + st * C::A_SLOT), &tmA, kb * TC_BK, c.rowA0 + c.mt * TC_BM, i == 0 ? 0 : i - S,
+                    fb);
+              ++ja;
+            } else {
+              mbar_expect_tx(fb, C::B_SLOT);
+              tma3d(smem_u32(ringB + st * C::B_SLOT), &tmB, kb * TC_BK, c.rowB0 + c.nt * C::BN, i - 1, fb);
+              ++jb;
+            }
+          }
+      }
+      // every issued load lands before the CTA exits
+      for (int q = (ja > C::RA ? ja - C::RA : 0); q < ja; ++q)
+        mbar_wait(smem_u32(&sh->fullA[q % C::RA]), (uint32_t)((q / C::RA) & 1), kWaitLimit);
+      for (int q = (jb > C::RB ? jb - C::RB : 0); q < jb; ++q)
+        mbar_wait(smem_u32(&sh->fullB[q % C::RB]), (uint32_t)((q / C::RB) & 1), kWaitLimit);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t id = idesc_bf16(TC_BM, C::BN);
+      int ja = 0, jb = 0, jt = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles_total && ok && !sh->abort; t += gridDim.x, ++jt) {
+        const TileCoord c = persist_tile(g, t, mtiles, ntiles);
+        const int b = jt & 1, use = jt >> 1;
+        if (use > 0 && !mbar_wait(smem_u32(&sh->accempty[b]), (uint32_t)((use - 1) & 1), kWaitLimit)) {
+          fail(sh, g.err, 2);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t dbuf = tmem + (uint32_t)b * buf_cols;
+        bool first = true;
+        for (int kb = c.kb0; kb < c.kb1 && ok; ++kb, ja += S, jb += S) {
+          for (int s = 1; s <= S && ok; ++s) {
+            const int qa = ja + s - 1;  // A_s
+            if (!mbar_wait(smem_u32(&sh->fullA[qa % C::RA]), (uint32_t)((qa / C::RA) & 1), kWaitLimit)) {
+              ok = false;
+              break;
+            }
+            const uint64_t da = sdesc(smem_u32(ringA + (qa % C::RA) * C::A_SLOT));
+            for (int tt = 1; tt <= S + 1 - s; ++tt) {
+              const int qb = jb + tt - 1;  // B_tt
+              if (s == 1 &&
+                  !mbar_wait(smem_u32(&sh->fullB[qb % C::RB]), (uint32_t)((qb / C::RB) & 1), kWaitLimit)) {
+                ok = false;
+                break;
+              }
+              asm volatile("tcgen05.fence::after_thread_sync;");
+              const uint64_t db = sdesc(smem_u32(ringB + (qb % C::RB) * C::B_SLOT));
+              const uint32_t dacc = dbuf + (uint32_t)((s + tt - 2) * C::BN);
+#pragma unroll
+              for (int k = 0; k < TC_BK / 16; ++k) {
+                const uint32_t accf = (first && s == 1 && k == 0) ? 0u : 1u;
+                umma(dacc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), id, accf);
+              }
+            }
+            if (!ok) break;
+            // A_s and B_(S+1-s) have had their last use in this K block
+            umma_commit(smem_u32(&sh->emptyA[qa % C::RA]));
+            umma_commit(smem_u32(&sh->emptyB[(jb + S - s) % C::RB]));
+          }
+          first = false;
+        }
+        if (!ok) {
+          fail(sh, g.err, 3);
+          break;
+        }
+        umma_commit(smem_u32(&sh->accfull[b]));
+      }
+      umma_commit(smem_u32(&sh->done));
+      mbar_wait(smem_u32(&sh->done), 0, kWaitLimit);
+    }
+  } else {
+    // ---------------- drain warps (2 .. 17): 16 columns each ----------------
+    const int q = warp & 3;
+    const int j0 = ((warp - 2) >> 2) * 16;  // this warp's packed columns
+    const int row = q * 32 + lane;
+    const bool odd = AC && (lane & 1);
+    constexpr int NJ = BC ? 8 : 16;        // logical columns of the group
+    constexpr int rows_out = AC ? 16 : 32;  // logical rows of this warp
+    constexpr int RS = NJ + 1;              // staging row stride, padded
+    constexpr bool REAL_ONLY = !AC && !BC;  // real operands: stage the real part only
+    double2* stage2 = reinterpret_cast<double2*>(stg + (size_t)(warp - 2) * C::STAGE_WARP);
+    double* stage1 = reinterpret_cast<double*>(stg + (size_t)(warp - 2) * C::STAGE_WARP);
+    const int lr = AC ? (lane >> 1) : lane;
+    const uint32_t tl = (uint32_t)(q * 32) << 16;
+    const int u = 7 * (S + 1);
+    const bool neg = g.alpha_pow2 && g.alpha_neg;
+    const bool red = g.acc || g.atomic;
+    constexpr int RPP = 32 / NJ;
+    constexpr int NPASS = rows_out / RPP;
+    const int lc = lane % NJ, lrw = lane / NJ;
+    int jt = 0;
+    for (int t = blockIdx.x; t < ntiles_total; t += gridDim.x, ++jt) {
+      const TileCoord c = persist_tile(g, t, mtiles, ntiles);
+      const int b = jt & 1, use = jt >> 1;
+      // one decision for all drain warps, and the tile's column data
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * C::EPI) : "memory");
+      const int td = threadIdx.x - 64;
+      if (td == 0) sh->stop = sh->abort;
+      {
+        constexpr int ncl = BC ? C::BN / 2 : C::BN;
+        if (td < ncl) {
+          const int n = c.nt * ncl + td;
+          long long o = -1;
+          if (n < g.N) decomp_tc(g.gnC, n, o);
+          sh->col_off[td] = o;
+        }
+        if (td < C::BN) sh->col_exp[td] = row_exp(g.expB[c.rowB0 + c.nt * C::BN + td]);
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * C::EPI) : "memory");
+      if (sh->stop) break;  // the same value for every drain warp
+      const bool got = mbar_wait(smem_u32(&sh->accfull[b]), (uint32_t)(use & 1), kWaitLimit);
+      if (!__all_sync(0xffffffffu, got)) {
+        fail(sh, g.err, 4);
+        continue;  // the next tile's decision stops every drain warp
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      long long a16[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) a16[j] = 0;
+#pragma unroll
+      for (int L0 = 2; L0 <= 5; L0 += 2) {
+        if (L0 > S + 1) break;
+        uint32_t lv[2][16];
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+          if (L0 + i <= S + 1)
+            tmem_ld16_nowait(tmem + tl + (uint32_t)b * buf_cols + (uint32_t)((L0 + i - 2) * C::BN + j0), lv[i]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const int L = L0 + i;
+          if (L > S + 1) break;
+          const int shl = u - 7 * L;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) a16[j] += (long long)__float2int_rn(__uint_as_float(lv[i][j])) << shl;
+        }
+      }
+      // the levels are in registers: the MMAs of a later tile may refill this buffer
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mbar_arrive(smem_u32(&sh->accempty[b]));
+      const int prow = c.mt * TC_BM + row;
+      const int m = AC ? (prow >> 1) : prow;
+      const int ea = prow < g.rowsA_pad ? row_exp(g.expA[c.rowA0 + prow]) : 0;
+      const int ebase = ea - u + (g.alpha_pow2 ? g.alpha_e : 0);
+      long long coffm = 0;
+      if (m < g.M) decomp_tc(g.gmC, m, coffm);
+      double2* Cc = static_cast<double2*>(g.C) + (g.cc ? c.zb * g.bsC : 0);
+      double* Cr = static_cast<double*>(g.C) + (g.cc ? 0 : c.zb * g.bsC);
+      const int m0w = AC ? ((c.mt * TC_BM + q * 32) >> 1) : (c.mt * TC_BM + q * 32);
+      const int nrows = min(rows_out, g.M - m0w);
+      __syncwarp();  // the previous tile's stores have read the staging area
+#pragma unroll
+      for (int k = 0; k < NJ; ++k) {
+        const int jj = (BC ? j0 / 2 : j0) + k;
+        long long re, im;
+        if constexpr (BC) {
+          const long long x0 = a16[2 * k], x1 = a16[2 * k + 1];
+          if constexpr (AC) {
+            const long long p0 = __shfl_xor_sync(0xffffffffu, x0, 1);
+            const long long p1 = __shfl_xor_sync(0xffffffffu, x1, 1);
+            const long long rr = odd ? p0 : x0, ri = odd ? p1 : x1, ir = odd ? x0 : p0, ii = odd ? x1 : p1;
+            re = rr - ii;
+            im = ri + ir;
+          } else {
+            re = x0;
+            im = x1;
+          }
+        } else {
+          const long long x = a16[k];
+          if constexpr (AC) {
+            const long long p = __shfl_xor_sync(0xffffffffu, x, 1);
+            re = odd ? p : x;
+            im = odd ? x : p;
+          } else {
+            re = x;
+            im = 0;
+          }
+        }
+        if (AC && ((k & 1) != (lane & 1))) continue;
+        const int E = ebase + sh->col_exp[BC ? 2 * jj : jj];
+        double vr, vi;
+        if (g.alpha_pow2) {
+          vr = scaled_i64_to_double(neg ? -re : re, E);
+          vi = scaled_i64_to_double(neg ? -im : im, E);
+        } else {
+          const double dr = scaled_i64_to_double(re, E), di = scaled_i64_to_double(im, E);
+          vr = g.ar * dr - g.ai * di;
+          vi = g.ar * di + g.ai * dr;
+        }
+        if constexpr (REAL_ONLY)
+          stage1[lr * RS + k] = vr;
+        else
+          stage2[lr * RS + k] = make_double2(vr, vi);
+      }
+      __syncwarp();
+      const long long cn = sh->col_off[(BC ? j0 / 2 : j0) + lc];
+#pragma unroll 4
+      for (int p = 0; p < NPASS; ++p) {
+        const int r = p * RPP + lrw;
+        const long long cm = __shfl_sync(0xffffffffu, coffm, (AC ? 2 * r : r) & 31);
+        if (r >= nrows || cn < 0) continue;
+        const long long off = cm + cn;
+        const double2 v = REAL_ONLY ? make_double2(stage1[r * RS + lc], 0.0) : stage2[r * RS + lc];
+        if (g.cc) {
+          if (red) {
+            atomicAdd(&Cc[off].x, v.x);
+            if (!REAL_ONLY) atomicAdd(&Cc[off].y, v.y);
+          } else {
+            Cc[off] = v;
+          }
+        } else {
+          if (red)
+            atomicAdd(&Cr[off], v.x);
+          else
+            Cr[off] = v.x;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+// ---------------------------------------------------------------------------
 // Short contractions (K <= 64) of the mixed mode on the FP32 pipe: the same
 // exact slice products as the tensor-core path, without packing.  One output
 // tile per block: the block takes the binary exponents of its rows of A and
@@ -1422,8 +1764,54 @@ static cudaError_t launch_tile128(const TcArgs& a0, const void* packA, const voi
   return cudaGetLastError();
 }
 
+static cudaError_t launch_persist(const TcArgs& a0, const void* packA, const void* packB, cudaStream_t st) {
+  using C = TcPersist;
+  constexpr int kMaxDev = 64;
+  static std::once_flag once[kMaxDev];
+  static cudaError_t attr_err[kMaxDev] = {};
+  static int sm_count[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+  std::call_once(once[dev], [dev] {
+    cudaError_t e = cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
+    for (auto fn : {ozaki_persist_kernel<true, true>, ozaki_persist_kernel<true, false>,
+                    ozaki_persist_kernel<false, true>, ozaki_persist_kernel<false, false>}) {
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    }
+    attr_err[dev] = e;
+  });
+  if (attr_err[dev] != cudaSuccess) return attr_err[dev];
+  TcArgs a = a0;
+  // two TMEM buffers of S levels, one exact K chunk per tile
+  if (a.S < 1 || a.S > TC_TILE128_MAX_S || a.kb_per_split > tc_chunk_kblocks(a.S)) return cudaErrorInvalidValue;
+  int cols = 32;
+  while (cols < 2 * a.S * C::BN) cols *= 2;
+  a.tmem_cols = cols;
+  if (a.rowsB_pad % C::BN != 0 || a.rowsA_pad % TC_BM != 0) return cudaErrorInvalidValue;
+  const CUtensorMap ma = slice_map(packA, a.S, (a.bat_a ? a.nb : 1) * a.rowsA_pad, a.kblocks * TC_BK, TC_BM);
+  const CUtensorMap mb = slice_map(packB, a.S, (a.bat_b ? a.nb : 1) * a.rowsB_pad, a.kblocks * TC_BK, C::BN);
+  const long long mtiles = a.rowsA_pad / TC_BM, ntiles = a.rowsB_pad / C::BN;
+  a.m_fast = a.rowsA_pad < a.rowsB_pad ? 1 : 0;
+  const long long total = mtiles * ntiles * a.nb * a.nsplit;
+  if (total > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;
+  const unsigned grid = (unsigned)std::min<long long>(total, std::max(sm_count[dev], 1));
+  if (a.ac && a.bc)
+    ozaki_persist_kernel<true, true><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a, (int)total);
+  else if (a.ac)
+    ozaki_persist_kernel<true, false><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a, (int)total);
+  else if (a.bc)
+    ozaki_persist_kernel<false, true><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a, (int)total);
+  else
+    ozaki_persist_kernel<false, false><<<grid, C::THREADS, C::SMEM, st>>>(ma, mb, a, (int)total);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ozaki(const TcArgs& a, const void* packA, const void* packB, cudaStream_t st) {
   if (a.nb < 1 || a.nsplit < 1 || (long long)a.nsplit * a.kb_per_split < a.kblocks) return cudaErrorInvalidValue;
+  if (a.variant == 3) return launch_persist(a, packA, packB, st);
   if (a.variant == 2) return launch_tile128(a, packA, packB, st);
   return a.variant == 1 ? launch_variant<TcNarrow>(a, packA, packB, st) : launch_variant<TcWide>(a, packA, packB, st);
 }

@@ -43,6 +43,23 @@ struct TcTile128 {
 };
 constexpr int TC_TILE128_MAX_S = 4;
 
+// Persistent 64-column form for S <= 4 slices: one CTA per SM walks a list
+// of output tiles; S level accumulators of 64 columns make one TMEM buffer
+// (S x 64 <= 256 columns), two buffers fill TMEM, so that the drain warps
+// empty tile i's buffer while the MMAs of tile i + 1 fill the other.  Slices
+// of A (128 x 64, 16 KB) and of B (64 x 64, 8 KB) have rings of their own;
+// the drain stages 16 columns per warp in an area of its own (the rings keep
+// loading the next tile meanwhile).
+struct TcPersist {
+  static constexpr int BN = 64, EPI = 16, MINB = 1;
+  static constexpr int RA = 5, RB = 6;               // ring slots of A and B slices
+  static constexpr int A_SLOT = TC_BM * TC_BK * 2;   // 16 KB
+  static constexpr int B_SLOT = BN * TC_BK * 2;      // 8 KB
+  static constexpr int STAGE_WARP = 4608;            // staging bytes per drain warp
+  static constexpr int THREADS = 64 + 32 * EPI;
+  static constexpr int SMEM = 1024 + RA * A_SLOT + RB * B_SLOT + EPI * STAGE_WARP + 2048;
+};
+
 // K blocks one CTA of the 128-wide tile may accumulate exactly: the FP32
 // level sums grow by at most sum_{s+t=L} |q_s| |q_t| per K index (|q_1| <=
 // 128, |q_s| <= 64 for s >= 2) and must stay within 2^24.

@@ -1111,8 +1111,14 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     // split K so that few output tiles still occupy the SMs: one CTA per SM,
     // cost = waves x (K blocks per CTA + fixed pipeline/epilogue overhead);
     // the 128-column tile takes at most one exact K chunk per CTA
-    const long long ctas = (rB / (tile128 ? TcTile128::BN : BN)) * (rA / BM) * nbt;
-    const long long min_sp = tile128 ? (a.kblocks + tc_chunk_kblocks(S) - 1) / tc_chunk_kblocks(S) : 1;
+    // S <= 4 and at most two K blocks: the persistent 64-column form, whose
+    // TMEM drain runs under the next tile's loads and MMAs (measured at o=10,
+    // v=38 with 24 trajectories: 10-35 % faster than the 128-column tile for
+    // one or two K blocks, 30-50 % slower for six or more, where the
+    // 128-column tile's MMA rate and operand reuse count)
+    const bool persist = S <= TC_TILE128_MAX_S && a.kblocks <= 2;
+    const long long ctas = (rB / (tile128 && !persist ? TcTile128::BN : BN)) * (rA / BM) * nbt;
+    const long long min_sp = (tile128 || persist) ? (a.kblocks + tc_chunk_kblocks(S) - 1) / tc_chunk_kblocks(S) : 1;
     long long splits = min_sp;
     {
       double best = 1e300;
@@ -1133,7 +1139,7 @@ void Program::select_backend(int prec_mode, long long min_macs, int S, int min_k
     a.atomic = splits > 1 ? 1 : 0;
     t.zeroed = a.acc || a.atomic;  // split K is allowed (a zero op precedes when not accumulating)
     // short K: the narrow variant (two CTAs per SM overlap their latencies)
-    a.variant = tile128 ? 2 : (a.kb_per_split == 1 && S <= 5) ? 1 : 0;
+    a.variant = persist ? 3 : tile128 ? 2 : (a.kb_per_split == 1 && S <= 5) ? 1 : 0;
     t.bytes = (long long)S * (nbA * rA + nbB * rB) * Kp * 2 + nbt * M * N * elem_bytes(op.dtc);
     t.reads = {pa.pk_dst, pb.pk_dst};
     if (a.acc || a.atomic) t.reads.push_back(op.sc);
