@@ -120,7 +120,11 @@ int tdcc_system_batch(tdcc_system s);   /* nb of the system (0 for NULL) */
 int tdcc_set_fields(tdcc_system s, const tdcc_field* fields, const int* pol);
 
 /* Selects the contraction arithmetic (TDCC_PREC_*) and, for the mixed mode,
-   the number of BF16 slices per operand (2..6; 7 bits each).             */
+   the number of BF16 slices per operand (2..6; 7 bits each).  With up to 4
+   slices the tensor-core products take the 128-column tile or, for one or
+   two K blocks, the persistent 64-column form; with 5 or 6 the 64-column
+   tile.  4 slices keep |d mu| within 1e-8 a.u. of the FP64 form over 2000
+   steps of the o=10, v=38 system; strongly correlated systems need 5.    */
 int tdcc_set_precision(tdcc_system s, int mode, int slices);
 
 /* Ground-state amplitudes by Jacobi sweeps with eigh(F) denominators and
