@@ -1329,11 +1329,15 @@ __global__ void __launch_bounds__(256, 2) simt_slices_kernel(const GemmArgs g, i
                                                              int alpha_neg) {
   constexpr int PA = AC ? 2 : 1, PB = BC ? 2 : 1;
   constexpr int SPA = (S * PA + 1) / 2 * 2, SPB = (S * PB + 1) / 2 * 2;  // floats per row, even
+  // shared row strides: B's columns are read by the 16 tx values of a half
+  // warp at once, so their stride is twice an odd number of floats (the 16
+  // float2 reads fall in distinct bank pairs); A's rows by two ty values only
+  constexpr int STA = SPA, STB = (SPB / 2) % 2 == 1 ? SPB : SPB + 2;
   constexpr int MI = BM / 16, NJ = BN / 16;
   static_assert(MI * NJ == 4, "four outputs per thread");
   constexpr int KC = (BM > 32 || BN > 32) ? 8 : 16;  // K chunk (static shared memory <= 48 KB)
-  __shared__ __align__(8) float sa[KC][BM][SPA];
-  __shared__ __align__(8) float sb[KC][BN][SPB];
+  __shared__ __align__(8) float sa[KC][BM][STA];
+  __shared__ __align__(8) float sb[KC][BN][STB];
   __shared__ long long aoff[BM], boff[BN], coffm[BM], coffn[BN];
   __shared__ long long kofa[kSimtMaxK], kofb[kSimtMaxK];
   __shared__ int ea[BM], eb[BN];
