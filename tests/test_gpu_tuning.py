@@ -1,6 +1,8 @@
 """Launch-shape and memory choices must not change results: workspace buffer
-sharing forced on, the autotuner's picks, and the two tensor-core kernel
-variants, against the default configuration (FP64 and mixed)."""
+sharing forced on, the autotuner's picks, and the tensor-core kernel forms
+(with 5 slices the 64- and 32-column tiles; with 4 the 128-column tile and
+the persistent 64-column form as well), against the default configuration
+(FP64 and mixed)."""
 import numpy as np
 import pytest
 
@@ -19,8 +21,8 @@ def _run(method, prec, nb, sharing=None, tune=False, steps=8):
     d, sysm = load("golden_o6_v10.npz")
     eng = CCEngine.from_system(sysm, nb=nb)
     try:
-        if prec == "mixed":
-            eng.set_precision("mixed", 5)
+        if prec.startswith("mixed"):
+            eng.set_precision("mixed", 4 if prec == "mixed4" else 5)
             eng.set_tc_policy(0, 1, 1)
         if sharing is not None:
             eng.set_memory_sharing(sharing)
@@ -37,7 +39,8 @@ def _run(method, prec, nb, sharing=None, tune=False, steps=8):
         eng.close()
 
 
-@pytest.mark.parametrize("method,prec,nb", [("CCSD", "fp64", 1), ("CCSD", "mixed", 3), ("CC2", "mixed", 2)])
+@pytest.mark.parametrize("method,prec,nb", [("CCSD", "fp64", 1), ("CCSD", "mixed", 3), ("CC2", "mixed", 2),
+                                            ("CCSD", "mixed4", 3)])
 def test_buffer_sharing_and_autotune_keep_results(method, prec, nb):
     ref_mu, ref_st = _run(method, prec, nb)
     for kw in ({"sharing": 0}, {"tune": True}, {"sharing": 0, "tune": True}):
