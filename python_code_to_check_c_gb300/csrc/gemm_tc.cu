@@ -56,6 +56,20 @@ namespace tdcc {
 // ---------------------------------------------------------------------------
 // packing
 // ---------------------------------------------------------------------------
+// Digits of two neighbouring elements of a packed row (same exponent e), one
+// BF16 pair per slice: out is the packed buffer as BF16 pairs, plane2 the
+// pairs per slice, idx2 the pair's index within a slice.
+__device__ __forceinline__ void store_digit_pair(uint32_t* out, size_t plane2, size_t idx2, double x0, double x1,
+                                                 int e, int nbits, int S) {
+  int q0[TC_MAX_SLICES], q1[TC_MAX_SLICES];
+  balanced_digits(fixed_point(x0, e, nbits), S, q0);
+  balanced_digits(fixed_point(x1, e, nbits), S, q1);
+  const bool n0 = __double_as_longlong(x0) < 0, n1 = __double_as_longlong(x1) < 0;  // sign bits
+#pragma unroll
+  for (int s = 0; s < TC_MAX_SLICES; ++s)
+    if (s < S) out[s * plane2 + idx2] = digit_pair_bf16x2(n0 ? -q0[s] : q0[s], n1 ? -q1[s] : q1[s]);
+}
+
 // One block per logical row (per batch; the real and imaginary rows of a
 // complex row together): pass 1 takes the binary exponent e of the row's
 // max |x| (max = f 2^e, f in [0.5, 1); integer ops on the bit patterns, the
@@ -118,52 +132,52 @@ __global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
   }
   const int e = row_exp(eb);
   const int nbits = 7 * p.S;
-  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
-  const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
-  for (int k0 = threadIdx.x; k0 < p.K_pad; k0 += U * blockDim.x) {
-    double x[U][2];
+  uint32_t* out = static_cast<uint32_t*>(p.out);  // BF16 pairs (K_pad is even)
+  const size_t plane2 = (size_t)p.nb * p.rows_pad * (p.K_pad / 2);
+  // pass 2 over pairs of neighbouring K indices (one 4-byte store per slice
+  // and part), two pairs per thread: four loads in flight
+  constexpr int U2 = 2;
+  for (int k0 = 2 * threadIdx.x; k0 < p.K_pad; k0 += 2 * U2 * blockDim.x) {
+    double x[U2][2][2];  // [pair][element][part]
 #pragma unroll
-    for (int j = 0; j < U; ++j) {
-      const int k = k0 + j * blockDim.x;
-      x[j][0] = x[j][1] = 0.0;
-      if (k < p.K) {
-        long long ko;
-        decomp_tc(p.gk, k, ko);
-        const long long el = ro + ko;
-        if (p.cplx) {
-          const double2 w = *reinterpret_cast<const double2*>(src + 2 * el);
-          x[j][0] = w.x;
-          x[j][1] = w.y;
-        } else {
-          x[j][0] = src[el];
+    for (int j = 0; j < U2; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = k0 + 2 * j * blockDim.x + h;
+        x[j][h][0] = x[j][h][1] = 0.0;
+        if (k < p.K) {
+          long long ko;
+          decomp_tc(p.gk, k, ko);
+          const long long el = ro + ko;
+          if (p.cplx) {
+            const double2 w = *reinterpret_cast<const double2*>(src + 2 * el);
+            x[j][h][0] = w.x;
+            x[j][h][1] = w.y;
+          } else {
+            x[j][h][0] = src[el];
+          }
         }
       }
-    }
 #pragma unroll
-    for (int j = 0; j < U; ++j) {
-      const int k = k0 + j * blockDim.x;
+    for (int j = 0; j < U2; ++j) {
+      const int k = k0 + 2 * j * blockDim.x;
       if (k >= p.K_pad) break;
-      for (int part = 0; part < per; ++part) {
-        const unsigned long long f = fixed_point(x[j][part], e, nbits);
-        const bool neg = __double_as_longlong(x[j][part]) < 0;  // sign bit: no FP64 compare
-        const size_t base = (prow + part) * p.K_pad + k;
-        int qd[TC_MAX_SLICES];
-        balanced_digits(f, p.S, qd);
-#pragma unroll
-        for (int s = 0; s < TC_MAX_SLICES; ++s)
-          if (s < p.S) out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -qd[s] : qd[s]));
-      }
+      for (int part = 0; part < per; ++part)
+        store_digit_pair(out, plane2, ((prow + part) * p.K_pad + k) / 2, x[j][0][part], x[j][1][part], e, nbits,
+                         p.S);
     }
   }
 }
 
 // Short rows (K_pad <= 32 * KW): one warp per logical row, eight rows per
-// block.  Each lane keeps its KW elements of the row in registers, so the
-// row is read once: the warp takes the exponent with shuffles and cuts the
-// digits from the registers (same exponent, digits and layout as
-// pack_kernel).
+// block.  Each lane keeps KW elements of the row in registers, KW / 2 pairs
+// of neighbours (pair lane + 32 j), so the row is read once: the warp takes
+// the exponent with shuffles and cuts the digits from the registers (same
+// exponent, digits and layout as pack_kernel).
 template <int KW>
 __global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
+  static_assert(KW % 2 == 0, "pairs of elements per lane");
+  constexpr int KP = KW / 2;
   const int per = p.cplx ? 2 : 1;
   const int lane = threadIdx.x & 31;
   const long long lr = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);  // logical row over all batches
@@ -174,27 +188,29 @@ __global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
   ro += z * p.bs;
   const double* src = static_cast<const double*>(p.src);
   constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
-  double x[KW][2];
+  double x[KP][2][2];  // [pair][element][part]
   unsigned long long mx = 0;
 #pragma unroll
-  for (int j = 0; j < KW; ++j) {
-    const int k = lane + 32 * j;
-    x[j][0] = x[j][1] = 0.0;
-    if (k < p.K) {
-      long long ko;
-      decomp_tc(p.gk, k, ko);
-      const long long el = ro + ko;
-      if (p.cplx) {
-        const double2 v = *reinterpret_cast<const double2*>(src + 2 * el);
-        x[j][0] = v.x;
-        x[j][1] = v.y;
-      } else {
-        x[j][0] = src[el];
+  for (int j = 0; j < KP; ++j)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 2 * (lane + 32 * j) + h;
+      x[j][h][0] = x[j][h][1] = 0.0;
+      if (k < p.K) {
+        long long ko;
+        decomp_tc(p.gk, k, ko);
+        const long long el = ro + ko;
+        if (p.cplx) {
+          const double2 v = *reinterpret_cast<const double2*>(src + 2 * el);
+          x[j][h][0] = v.x;
+          x[j][h][1] = v.y;
+        } else {
+          x[j][h][0] = src[el];
+        }
       }
+      mx = max(mx, max((unsigned long long)__double_as_longlong(x[j][h][0]) & kAbs,
+                       (unsigned long long)__double_as_longlong(x[j][h][1]) & kAbs));
     }
-    mx = max(mx, max((unsigned long long)__double_as_longlong(x[j][0]) & kAbs,
-                     (unsigned long long)__double_as_longlong(x[j][1]) & kAbs));
-  }
   for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
   const int E = (int)(mx >> 52);
   const int eb = mx != 0 ? (E > 0 ? E - 1022 : -1022) + kExpBias : 0;
@@ -205,22 +221,14 @@ __global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
   }
   const int e = row_exp(eb);
   const int nbits = 7 * p.S;
-  __nv_bfloat16* out = reinterpret_cast<__nv_bfloat16*>(p.out);
-  const size_t plane = (size_t)p.nb * p.rows_pad * p.K_pad;
+  uint32_t* out = static_cast<uint32_t*>(p.out);  // BF16 pairs (K_pad is even)
+  const size_t plane2 = (size_t)p.nb * p.rows_pad * (p.K_pad / 2);
 #pragma unroll
-  for (int j = 0; j < KW; ++j) {
-    const int k = lane + 32 * j;
+  for (int j = 0; j < KP; ++j) {
+    const int k = 2 * (lane + 32 * j);
     if (k >= p.K_pad) break;
-    for (int part = 0; part < per; ++part) {
-      const unsigned long long f = fixed_point(x[j][part], e, nbits);
-      const bool neg = __double_as_longlong(x[j][part]) < 0;
-      const size_t base = (prow + part) * p.K_pad + k;
-      int qd[TC_MAX_SLICES];
-      balanced_digits(f, p.S, qd);
-#pragma unroll
-      for (int s = 0; s < TC_MAX_SLICES; ++s)
-        if (s < p.S) out[s * plane + base] = __float2bfloat16_rn((float)(neg ? -qd[s] : qd[s]));
-    }
+    for (int part = 0; part < per; ++part)
+      store_digit_pair(out, plane2, ((prow + part) * p.K_pad + k) / 2, x[j][0][part], x[j][1][part], e, nbits, p.S);
   }
 }
 
@@ -1436,7 +1444,7 @@ __global__ void __launch_bounds__(256, 2) simt_slices_kernel(const GemmArgs g, i
         int qd[S];
         balanced_digits(f, S, qd);
 #pragma unroll
-        for (int s = 0; s < S; ++s) dst[s * per + part] = (float)(neg ? -qd[s] : qd[s]);
+        for (int s = 0; s < S; ++s) dst[s * per + part] = small_int_to_float(neg ? -qd[s] : qd[s]);
       }
     }
     __syncthreads();
@@ -1639,7 +1647,8 @@ static CUtensorMap slice_map(const void* base, int S, int rows_pad, int K_pad, i
 }
 
 cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
-  if (p.nb < 1 || p.rows < 1 || p.rows_pad % (p.cplx ? 2 : 1) != 0 || p.rows * (p.cplx ? 2 : 1) > p.rows_pad)
+  if (p.nb < 1 || p.rows < 1 || p.rows_pad % (p.cplx ? 2 : 1) != 0 || p.rows * (p.cplx ? 2 : 1) > p.rows_pad ||
+      p.K_pad % 2 != 0 || p.K > p.K_pad)
     return cudaErrorInvalidValue;
   const long long blocks = (long long)p.nb * p.rows;
   if (blocks > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;

@@ -65,6 +65,22 @@ __device__ __forceinline__ void balanced_digits(unsigned long long f, int S, int
   q[0] = (int)f;
 }
 
+// (float)d for |d| < 2^22 with one integer and one FP32 addition, both on
+// full-rate pipes (an int-to-float conversion runs at a quarter of that):
+// 0x4B400000 is the float 1.5 * 2^23, whose neighbours are 1 apart, so its
+// bits + d are the float 1.5 * 2^23 + d, and the subtraction is exact.  d = 0
+// gives +0, as the conversion does.
+__device__ __forceinline__ float small_int_to_float(int d) {
+  return __int_as_float(0x4B400000 + d) - 12582912.0f;
+}
+
+// Two digits (|d| <= 128, at most 8 significant bits: exact in BF16, whose
+// bits are then the upper half of the float's) as a BF16 pair, d0 in the low
+// half (the lower address).
+__device__ __forceinline__ uint32_t digit_pair_bf16x2(int d0, int d1) {
+  return __byte_perm(__float_as_uint(small_int_to_float(d0)), __float_as_uint(small_int_to_float(d1)), 0x7632);
+}
+
 // Subnormal or overflowing results (not met by the contractions here) take
 // the FP64 path, out of line so that nothing of it is evaluated on the
 // normal path.
