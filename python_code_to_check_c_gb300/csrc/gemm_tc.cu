@@ -169,20 +169,22 @@ __global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
   }
 }
 
-// Short rows (K_pad <= 32 * KW): one warp per logical row, eight rows per
-// block.  Each lane keeps KW elements of the row in registers, KW / 2 pairs
-// of neighbours (pair lane + 32 j), so the row is read once: the warp takes
-// the exponent with shuffles and cuts the digits from the registers (same
-// exponent, digits and layout as pack_kernel).
-template <int KW>
-__global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
-  static_assert(KW % 2 == 0, "pairs of elements per lane");
-  constexpr int KP = KW / 2;
+// Rows of up to 64 W KP elements: W warps per logical row, 8 / W rows per
+// 256-thread block.  Each lane keeps KP pairs of neighbours in registers
+// (pair index 32 w + lane + 32 W j for warp w of the row), so the row is read
+// once: the exponent comes from shuffles (and shared memory across the W
+// warps), the digits from the registers (same exponent, digits and layout as
+// pack_kernel).
+template <int KP, int W>
+__global__ void __launch_bounds__(256) pack_rows_regs_kernel(const PackArgs p) {
+  static_assert(W == 1 || W == 2 || W == 4 || W == 8, "warps per row divide the block");
+  constexpr int RPB = 8 / W;
   const int per = p.cplx ? 2 : 1;
-  const int lane = threadIdx.x & 31;
-  const long long lr = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);  // logical row over all batches
-  if (lr >= (long long)p.nb * p.rows) return;  // warp-uniform
-  const int z = (int)(lr / p.rows), m = (int)(lr - (long long)z * p.rows);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wr = warp % W;  // warp within the row
+  const long long lr = (long long)blockIdx.x * RPB + warp / W;  // logical row over all batches
+  const bool live = lr < (long long)p.nb * p.rows;              // uniform over the row's warps
+  const int z = live ? (int)(lr / p.rows) : 0, m = live ? (int)(lr - (long long)z * p.rows) : 0;
   long long ro = 0;
   decomp_tc(p.gr, m, ro);
   ro += z * p.bs;
@@ -194,9 +196,9 @@ __global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
   for (int j = 0; j < KP; ++j)
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int k = 2 * (lane + 32 * j) + h;
+      const int k = 2 * (32 * wr + lane + 32 * W * j) + h;
       x[j][h][0] = x[j][h][1] = 0.0;
-      if (k < p.K) {
+      if (live && k < p.K) {
         long long ko;
         decomp_tc(p.gk, k, ko);
         const long long el = ro + ko;
@@ -212,10 +214,19 @@ __global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
                        (unsigned long long)__double_as_longlong(x[j][h][1]) & kAbs));
     }
   for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+  if (W > 1) {
+    __shared__ unsigned long long wmax[8];
+    if (lane == 0) wmax[warp] = mx;
+    __syncthreads();  // every thread of the block arrives (no return above)
+    const int w0 = warp - wr;
+#pragma unroll
+    for (int w = 0; w < W; ++w) mx = max(mx, wmax[w0 + w]);
+  }
+  if (!live) return;
   const int E = (int)(mx >> 52);
   const int eb = mx != 0 ? (E > 0 ? E - 1022 : -1022) + kExpBias : 0;
   const size_t prow = (size_t)z * p.rows_pad + (size_t)m * per;
-  if (lane == 0) {
+  if (wr == 0 && lane == 0) {
     p.exps[prow] = eb;
     if (p.cplx) p.exps[prow + 1] = eb;
   }
@@ -225,7 +236,7 @@ __global__ void __launch_bounds__(256) pack_rows_warp_kernel(const PackArgs p) {
   const size_t plane2 = (size_t)p.nb * p.rows_pad * (p.K_pad / 2);
 #pragma unroll
   for (int j = 0; j < KP; ++j) {
-    const int k = 2 * (lane + 32 * j);
+    const int k = 2 * (32 * wr + lane + 32 * W * j);
     if (k >= p.K_pad) break;
     for (int part = 0; part < per; ++part)
       store_digit_pair(out, plane2, ((prow + part) * p.K_pad + k) / 2, x[j][0][part], x[j][1][part], e, nbits, p.S);
@@ -1652,15 +1663,24 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
     return cudaErrorInvalidValue;
   const long long blocks = (long long)p.nb * p.rows;
   if (blocks > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;
-  if (p.K_pad <= 256) {
-    // short rows: a warp per row, eight rows per block, one read of the row
-    const unsigned grid = (unsigned)((blocks + 7) / 8);
+  if (p.K_pad <= 2048) {
+    // rows held in registers, read once: up to 256 elements per warp (8 per
+    // lane), up to eight warps per row
+    auto go = [&](auto kern, int rows_per_block) {
+      kern<<<(unsigned)((blocks + rows_per_block - 1) / rows_per_block), 256, 0, st>>>(p);
+    };
     if (p.K_pad <= 64)
-      pack_rows_warp_kernel<2><<<grid, 256, 0, st>>>(p);
+      go(pack_rows_regs_kernel<1, 1>, 8);
     else if (p.K_pad <= 128)
-      pack_rows_warp_kernel<4><<<grid, 256, 0, st>>>(p);
+      go(pack_rows_regs_kernel<2, 1>, 8);
+    else if (p.K_pad <= 256)
+      go(pack_rows_regs_kernel<4, 1>, 8);
+    else if (p.K_pad <= 512)
+      go(pack_rows_regs_kernel<4, 2>, 4);
+    else if (p.K_pad <= 1024)
+      go(pack_rows_regs_kernel<4, 4>, 2);
     else
-      pack_rows_warp_kernel<8><<<grid, 256, 0, st>>>(p);
+      go(pack_rows_regs_kernel<4, 8>, 1);
   } else {
     // long rows: a block per row; few long rows (the K = o v^2 operands)
     // take more threads per row so that the SMs still fill
