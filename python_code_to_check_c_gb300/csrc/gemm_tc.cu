@@ -40,6 +40,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <map>
 #include <mutex>
@@ -83,12 +84,30 @@ __device__ __forceinline__ void store_digit_pair(uint32_t* out, size_t plane2, s
 // are not written at all: they only feed accumulator rows (A) or columns (B)
 // that the product kernel never stores, and their exponent entries only
 // scale those values, so whatever the buffer holds there is harmless.
-__global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
+// With tab set, the K offsets (the same for every row) are decoded once per
+// block into shared memory as 32-bit integers (K of them) and both passes
+// read them there.
+__global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p, int tab) {
+  extern __shared__ int kofs[];
   const int per = p.cplx ? 2 : 1;
   const int z = blockIdx.x / p.rows, m = blockIdx.x - z * p.rows;  // one block per live row
   long long ro = 0;
   decomp_tc(p.gr, m, ro);
   ro += z * p.bs;
+  if (tab) {
+    for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
+      long long ko;
+      decomp_tc(p.gk, k, ko);
+      kofs[k] = (int)ko;
+    }
+    __syncthreads();
+  }
+  auto koff = [&](int k) -> long long {
+    if (tab) return kofs[k];
+    long long ko;
+    decomp_tc(p.gk, k, ko);
+    return ko;
+  };
   const unsigned long long* bits = static_cast<const unsigned long long*>(p.src);
   const double* src = static_cast<const double*>(p.src);
   constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
@@ -102,9 +121,7 @@ __global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
       const int k = k0 + j * blockDim.x;
       v[j][0] = v[j][1] = 0ull;
       if (k < p.K) {
-        long long ko;
-        decomp_tc(p.gk, k, ko);
-        const long long e = ro + ko;
+        const long long e = ro + koff(k);
         if (p.cplx) {
           const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(bits + 2 * e);
           v[j][0] = w.x;
@@ -146,9 +163,7 @@ __global__ void __launch_bounds__(1024) pack_kernel(const PackArgs p) {
         const int k = k0 + 2 * j * blockDim.x + h;
         x[j][h][0] = x[j][h][1] = 0.0;
         if (k < p.K) {
-          long long ko;
-          decomp_tc(p.gk, k, ko);
-          const long long el = ro + ko;
+          const long long el = ro + koff(k);
           if (p.cplx) {
             const double2 w = *reinterpret_cast<const double2*>(src + 2 * el);
             x[j][h][0] = w.x;
@@ -1685,7 +1700,22 @@ cudaError_t launch_pack(const PackArgs& p, cudaStream_t st) {
     // long rows: a block per row; few long rows (the K = o v^2 operands)
     // take more threads per row so that the SMs still fill
     const int threads = (p.K_pad >= 4096 && blocks < 4 * 152) ? 1024 : 256;
-    pack_kernel<<<(unsigned)blocks, threads, 0, st>>>(p);
+    // the K offsets as a shared-memory table when they fit (64 KB, 32 bits)
+    constexpr int kTabMax = 16384;
+    constexpr int kMaxDev = 64;
+    static std::once_flag once[kMaxDev];
+    static cudaError_t attr_err[kMaxDev] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    std::call_once(once[dev], [dev] {
+      attr_err[dev] = cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           kTabMax * (int)sizeof(int));
+    });
+    long long span = 0;  // largest K offset
+    for (int q = 0; q < p.gk.n && q < kMaxModes; ++q) span += (long long)(p.gk.dim[q] - 1) * std::llabs(p.gk.s0[q]);
+    const int tab = (attr_err[dev] == cudaSuccess && p.K <= kTabMax && span < (1LL << 31)) ? 1 : 0;
+    const size_t smem = tab ? (size_t)p.K * sizeof(int) : 0;
+    pack_kernel<<<(unsigned)blocks, threads, smem, st>>>(p, tab);
   }
   count_launch();
   return cudaGetLastError();

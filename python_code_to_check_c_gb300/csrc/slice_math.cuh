@@ -10,6 +10,7 @@
 
 namespace tdcc {
 
+// Offset of index l < prod(dim) of a mode group (last mode fastest).
 __device__ __forceinline__ void decomp_tc(const ModeGroup& g, int l, long long& o0) {
   if (g.n == 1) {  // l < dim[0]: no division
     o0 = (long long)l * g.s0[0];
@@ -17,7 +18,7 @@ __device__ __forceinline__ void decomp_tc(const ModeGroup& g, int l, long long& 
   }
   o0 = 0;
 #pragma unroll
-  for (int q = kMaxModes - 1; q >= 0; --q) {
+  for (int q = kMaxModes - 1; q >= 1; --q) {
     if (q < g.n) {
       const int d = g.dim[q];
       const int r = l % d;
@@ -25,6 +26,7 @@ __device__ __forceinline__ void decomp_tc(const ModeGroup& g, int l, long long& 
       o0 += (long long)r * g.s0[q];
     }
   }
+  o0 += (long long)l * g.s0[0];  // l < dim[0]: the outermost mode needs no division
 }
 
 // Row exponents are stored biased (e + kExpBias; 0 = all-zero row) so that
